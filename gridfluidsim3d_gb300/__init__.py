@@ -1,0 +1,15 @@
+"""gridfluidsim3d_gb300 -- GB300-native (sm_103a) per-substep FLIP core of
+GridFluidSim3D: P2G velocity splat, MICCG(0) pressure projection, PIC/FLIP G2P
+with RK4 advection, behind the reference's interfaces.
+
+The compute path is libgfs.so (CUDA kernels + C ABI, include/gfs.h).  This
+package is its host-side mirror; importing it needs no GPU, calling into it
+does, and there is no CPU fallback.
+"""
+from ._lib import GFSError, PRECISION_MIXED, PRECISION_PLAIN  # noqa: F401
+from .core import (AIR, FLUID, SOLID, CLScalarField, Context, FluidSimulation,  # noqa: F401
+                   MACVelocityField, ParticleAdvector, PressureSolver, PressureSolverParameters, face_shape)
+
+__all__ = ["GFSError", "PRECISION_PLAIN", "PRECISION_MIXED", "AIR", "FLUID", "SOLID", "Context",
+           "CLScalarField", "ParticleAdvector", "PressureSolver", "PressureSolverParameters",
+           "MACVelocityField", "FluidSimulation", "face_shape"]

@@ -1,0 +1,401 @@
+"""Host-side mirror of the reference's interfaces for the FLIP substep path.
+
+The classes keep the names and argument meaning of the reference's C++ /
+pyfluid API and forward to libgfs's C ABI:
+
+* ``CLScalarField``     -- CLScalarField (clscalarfield.h:67-125): point splats
+* ``ParticleAdvector``  -- ParticleAdvector (particleadvector.h:62-110):
+                           tricubic interpolation and RK1..RK4 advection
+* ``PressureSolver``    -- PressureSolver::solve (pressuresolver.h:113-117) with
+                           ``PressureSolverParameters`` (:38-47)
+* ``MACVelocityField``  -- the three face grids (macvelocityfield.h)
+* ``FluidSimulation``   -- the device-resident substep behind a subset of
+                           pyfluid's FluidSimulation (pyfluid/fluidsimulation.py):
+                           ``update(dt)`` runs one substep of the full frame dt,
+                           as the reference does (its CFL limit never binds,
+                           fluidsimulation.cpp:3392-3451).
+
+Arrays are numpy, laid out like the reference's Array3d (index i + W*(j + H*k),
+numpy shape (k, j, i)).  Errors raise GFSError (a RuntimeError), as pyfluid
+raises RuntimeError from its bindings.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import GFSError, PRECISION_MIXED, PRECISION_PLAIN, SimParams, StepStats
+
+AIR, FLUID, SOLID = 0, 1, 2
+
+
+def _arr(a, dtype, shape=None, name="array"):
+    a = np.asarray(a)
+    if a.dtype != dtype or not a.flags.c_contiguous:
+        a = np.ascontiguousarray(a, dtype=dtype)
+    if shape is not None and a.size != int(np.prod(shape)):
+        raise GFSError(_lib.GFS_ERR_INVALID, name, f"expected {int(np.prod(shape))} elements, got {a.size}")
+    return a
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def face_shape(d, isize, jsize, ksize):
+    return (ksize + (d == 2), jsize + (d == 1), isize + (d == 0))
+
+
+class Context:
+    """One CUDA device and stream (replaces the reference's OpenCL set-up)."""
+
+    _default = None
+
+    def __init__(self, device: int = 0):
+        L = _lib.lib()
+        h = ctypes.c_void_p()
+        L.gfs_ctx_create(device, ctypes.byref(h))
+        self._h = h
+        self.device = device
+
+    @classmethod
+    def default(cls) -> "Context":
+        if cls._default is None:
+            cls._default = Context(0)
+        return cls._default
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        _lib.lib().gfs_ctx_stream(self._h, ctypes.byref(s))
+        return s.value or 0
+
+    def synchronize(self):
+        _lib.lib().gfs_ctx_synchronize(self._h)
+
+    def device_name(self) -> str:
+        buf = ctypes.create_string_buffer(256)
+        _lib.lib().gfs_ctx_device_name(self._h, buf, 256)
+        return buf.value.decode()
+
+    def launch_count(self) -> int:
+        c = ctypes.c_int64()
+        _lib.lib().gfs_ctx_launch_count(self._h, ctypes.byref(c))
+        return c.value
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.lib().gfs_ctx_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MACVelocityField:
+    """U (ni+1, nj, nk), V (ni, nj+1, nk), W (ni, nj, nk+1) float grids."""
+
+    def __init__(self, isize, jsize, ksize, dx, u=None, v=None, w=None):
+        self.isize, self.jsize, self.ksize, self.dx = int(isize), int(jsize), int(ksize), float(dx)
+        dims = (self.isize, self.jsize, self.ksize)
+        self.u = _arr(u, np.float32, face_shape(0, *dims), "U").reshape(face_shape(0, *dims)) if u is not None \
+            else np.zeros(face_shape(0, *dims), np.float32)
+        self.v = _arr(v, np.float32, face_shape(1, *dims), "V").reshape(face_shape(1, *dims)) if v is not None \
+            else np.zeros(face_shape(1, *dims), np.float32)
+        self.w = _arr(w, np.float32, face_shape(2, *dims), "W").reshape(face_shape(2, *dims)) if w is not None \
+            else np.zeros(face_shape(2, *dims), np.float32)
+
+    def get_grid_dimensions(self):
+        return self.isize, self.jsize, self.ksize
+
+    def get_grid_cell_size(self):
+        return self.dx
+
+
+class CLScalarField:
+    """Splat accelerator (CLScalarField, clscalarfield.h:67-125), CUDA backed."""
+
+    def __init__(self, ctx: Context | None = None):
+        self.ctx = ctx or Context.default()
+        self._initialized = False
+
+    def initialize(self) -> bool:
+        self._initialized = True
+        return True
+
+    def add_point_values(self, points, values, radius, offset, dx, scalarfield, weightfield=None):
+        """Add sum(w*v) into scalarfield (and sum(w) into weightfield) for every node
+        within `radius` of point - offset (clscalarfield.cpp:200-267)."""
+        pts = _arr(points, np.float32).reshape(-1, 3)
+        vals = _arr(values, np.float32)
+        if len(vals) != len(pts):
+            raise GFSError(_lib.GFS_ERR_INVALID, "add_point_values", "points and values differ in length")
+        if scalarfield.dtype != np.float32 or not scalarfield.flags.c_contiguous:
+            raise GFSError(_lib.GFS_ERR_INVALID, "add_point_values", "scalarfield must be contiguous float32")
+        D, H, W = scalarfield.shape
+        off = _arr(offset, np.float32)
+        _lib.lib().gfs_scalar_field_add_point_values(self.ctx.handle, _p(pts), _p(vals), len(pts), float(radius),
+                                                     _p(off), float(dx), W, H, D, _p(scalarfield),
+                                                     _p(weightfield) if weightfield is not None else None)
+
+    def velocity_scalar_field(self, dir_, isize, jsize, ksize, dx, positions, velocities):
+        """FluidSimulation::_computeVelocityScalarField for one MAC component:
+        returns (field, is_set)."""
+        pos = _arr(positions, np.float32).reshape(-1, 3)
+        vel = _arr(velocities, np.float32).reshape(-1, 3)
+        shape = face_shape(dir_, isize, jsize, ksize)
+        field = np.zeros(shape, np.float32)
+        is_set = np.zeros(shape, np.uint8)
+        _lib.lib().gfs_velocity_scalar_field(self.ctx.handle, dir_, isize, jsize, ksize, float(dx), _p(pos), _p(vel),
+                                             len(pos), _p(field), _p(is_set))
+        return field, is_set.astype(bool)
+
+
+class ParticleAdvector:
+    """G2P sampling and RK advection (ParticleAdvector, particleadvector.h:62-110)."""
+
+    def __init__(self, ctx: Context | None = None):
+        self.ctx = ctx or Context.default()
+
+    def initialize(self) -> bool:
+        return True
+
+    def _field(self, vfield: MACVelocityField):
+        return (vfield.isize, vfield.jsize, vfield.ksize, vfield.dx, _arr(vfield.u, np.float32),
+                _arr(vfield.v, np.float32), _arr(vfield.w, np.float32))
+
+    def tricubic_interpolate(self, particles, vfield: MACVelocityField):
+        pts = _arr(particles, np.float32).reshape(-1, 3)
+        out = np.zeros_like(pts)
+        ni, nj, nk, dx, u, v, w = self._field(vfield)
+        _lib.lib().gfs_tricubic_interpolate(self.ctx.handle, ni, nj, nk, dx, _p(u), _p(v), _p(w), _p(pts), len(pts),
+                                            _p(out))
+        return out
+
+    def _advect(self, order, particles, vfield, dt):
+        pts = _arr(particles, np.float32).reshape(-1, 3)
+        out = np.zeros_like(pts)
+        ni, nj, nk, dx, u, v, w = self._field(vfield)
+        _lib.lib().gfs_advect_particles(self.ctx.handle, order, ni, nj, nk, dx, _p(u), _p(v), _p(w), float(dt),
+                                        _p(pts), len(pts), _p(out))
+        return out
+
+    def advect_particles_rk4(self, particles, vfield, dt):
+        return self._advect(4, particles, vfield, dt)
+
+    def advect_particles_rk3(self, particles, vfield, dt):
+        return self._advect(3, particles, vfield, dt)
+
+    def advect_particles_rk2(self, particles, vfield, dt):
+        return self._advect(2, particles, vfield, dt)
+
+    def advect_particles_rk1(self, particles, vfield, dt):
+        return self._advect(1, particles, vfield, dt)
+
+
+class PressureSolverParameters:
+    """PressureSolverParameters (pressuresolver.h:38-47).  The fluid cells are the
+    material grid's fluid cells in lexicographic order."""
+
+    def __init__(self, cellwidth, density, delta_time, material_grid, velocity_field: MACVelocityField):
+        self.cellwidth = float(cellwidth)
+        self.density = float(density)
+        self.delta_time = float(delta_time)
+        self.material_grid = material_grid
+        self.velocity_field = velocity_field
+
+
+class PressureSolver:
+    """MICCG(0) pressure solve (PressureSolver::solve, pressuresolver.cpp:116)."""
+
+    def __init__(self, ctx: Context | None = None, precision: int = PRECISION_PLAIN, tol: float = 1e-6,
+                 max_iterations: int = 200):
+        self.ctx = ctx or Context.default()
+        self.precision = precision
+        self.tol = tol
+        self.max_iterations = max_iterations
+        self.iterations = None
+        self.max_residual = None
+
+    def solve(self, params: PressureSolverParameters):
+        vf = params.velocity_field
+        mat = _arr(params.material_grid, np.uint8)
+        F = ctypes.c_int64(0)
+        L = _lib.lib()
+        ni, nj, nk = vf.isize, vf.jsize, vf.ksize
+        L.gfs_pressure_solve(self.ctx.handle, ni, nj, nk, params.cellwidth, params.density, params.delta_time,
+                             _p(mat), None, None, None, self.precision, self.tol, self.max_iterations, None,
+                             ctypes.byref(F), None, None)
+        out = np.zeros(max(F.value, 1), np.float64)
+        it = ctypes.c_int(0)
+        res = ctypes.c_double(0.0)
+        u, v, w = (_arr(a, np.float32) for a in (vf.u, vf.v, vf.w))
+        L.gfs_pressure_solve(self.ctx.handle, ni, nj, nk, params.cellwidth, params.density, params.delta_time,
+                             _p(mat), _p(u), _p(v), _p(w), self.precision, self.tol, self.max_iterations, _p(out),
+                             ctypes.byref(F), ctypes.byref(it), ctypes.byref(res))
+        self.iterations = it.value
+        self.max_residual = res.value
+        return out[:F.value]
+
+
+class FluidSimulation:
+    """Device-resident FLIP simulation behind a subset of pyfluid's FluidSimulation.
+
+    ``update(dt)`` runs one substep of length dt (stages 1, 5-9, 11, 12 of
+    FluidSimulation::_stepFluid); meshing, level set, diffuse particles, fluid
+    sources and autosave are not part of this core.
+    """
+
+    def __init__(self, isize, jsize, ksize, dx, max_particles, ctx: Context | None = None):
+        self.ctx = ctx or Context.default()
+        self.isize, self.jsize, self.ksize, self.dx = int(isize), int(jsize), int(ksize), float(dx)
+        h = ctypes.c_void_p()
+        _lib.lib().gfs_sim_create(self.ctx.handle, self.isize, self.jsize, self.ksize, self.dx, int(max_particles),
+                                  ctypes.byref(h))
+        self._h = h
+        self._params = SimParams()
+        _lib.lib().gfs_sim_default_params(ctypes.byref(self._params))
+        self.last_stats = None
+        self.current_frame = 0
+
+    # -- parameters (fluidsimulation.h:146-446 setters) --
+    def _push(self):
+        _lib.lib().gfs_sim_set_params(self._h, ctypes.byref(self._params))
+
+    @property
+    def density(self):
+        return self._params.density
+
+    @density.setter
+    def density(self, value):
+        if not value > 0:
+            raise GFSError(_lib.GFS_ERR_INVALID, "density", "must be > 0")
+        self._params.density = float(value)
+        self._push()
+
+    @property
+    def precision(self):
+        return self._params.precision
+
+    @precision.setter
+    def precision(self, value):
+        self._params.precision = int(value)
+        self._push()
+
+    @property
+    def pressure_tolerance(self):
+        return self._params.tol
+
+    @pressure_tolerance.setter
+    def pressure_tolerance(self, value):
+        self._params.tol = float(value)
+        self._push()
+
+    @property
+    def max_cg_iterations(self):
+        return self._params.max_cg_iterations
+
+    @max_cg_iterations.setter
+    def max_cg_iterations(self, value):
+        self._params.max_cg_iterations = int(value)
+        self._push()
+
+    def add_body_force(self, fx, fy=None, fz=None):
+        if fy is None:
+            fx, fy, fz = fx
+        g = self._params.gravity
+        self._params.gravity = (ctypes.c_float * 3)(g[0] + fx, g[1] + fy, g[2] + fz)
+        self._push()
+
+    def reset_body_force(self):
+        self._params.gravity = (ctypes.c_float * 3)(0.0, 0.0, 0.0)
+        self._push()
+
+    # -- state --
+    def set_material_grid(self, mat):
+        mat = _arr(mat, np.uint8, (self.ksize, self.jsize, self.isize), "material")
+        _lib.lib().gfs_sim_set_material(self._h, _p(mat))
+
+    def get_material_grid(self):
+        out = np.zeros((self.ksize, self.jsize, self.isize), np.uint8)
+        _lib.lib().gfs_sim_get_material(self._h, _p(out))
+        return out
+
+    def set_marker_particles(self, positions, velocities=None, ids=None):
+        pos = _arr(positions, np.float32).reshape(-1, 3)
+        vel = _arr(velocities, np.float32).reshape(-1, 3) if velocities is not None else None
+        idv = _arr(ids, np.uint32) if ids is not None else None
+        _lib.lib().gfs_sim_set_particles(self._h, _p(pos), _p(vel), _p(idv), len(pos))
+
+    def get_num_marker_particles(self) -> int:
+        n = ctypes.c_int64(0)
+        _lib.lib().gfs_sim_num_particles(self._h, ctypes.byref(n))
+        return n.value
+
+    def get_marker_particles(self):
+        """(positions, velocities, ids) in the device's (cell, id) order."""
+        n = self.get_num_marker_particles()
+        pos = np.zeros((n, 3), np.float32)
+        vel = np.zeros((n, 3), np.float32)
+        ids = np.zeros(n, np.uint32)
+        nn = ctypes.c_int64(0)
+        if n:
+            _lib.lib().gfs_sim_get_particles(self._h, _p(pos), _p(vel), _p(ids), ctypes.byref(nn))
+        return pos, vel, ids
+
+    def get_marker_particle_positions(self):
+        return self.get_marker_particles()[0]
+
+    def get_marker_particle_velocities(self):
+        return self.get_marker_particles()[1]
+
+    def get_velocity_field(self) -> MACVelocityField:
+        f = MACVelocityField(self.isize, self.jsize, self.ksize, self.dx)
+        _lib.lib().gfs_sim_get_velocity_field(self._h, _p(f.u), _p(f.v), _p(f.w))
+        return f
+
+    def get_pressure_grid(self):
+        out = np.zeros((self.ksize, self.jsize, self.isize), np.float32)
+        _lib.lib().gfs_sim_get_pressure_grid(self._h, _p(out))
+        return out
+
+    # -- stepping --
+    def update(self, dt) -> dict:
+        """One substep of length dt (FluidSimulation::update, fluidsimulation.cpp:3417-3455)."""
+        if dt < 0.0:
+            raise GFSError(_lib.GFS_ERR_INVALID, "update", f"delta time must be >= 0 (got {dt})")
+        st = StepStats()
+        _lib.lib().gfs_sim_step(self._h, float(dt), ctypes.byref(st))
+        self.last_stats = st.as_dict()
+        self.current_frame += 1
+        return self.last_stats
+
+    def update_host(self, dt, positions, velocities, ids):
+        """The same substep on host-resident particle arrays (copied in and out):
+        arrays are updated in place; returns (count, stats)."""
+        n = ctypes.c_int64(len(positions))
+        st = StepStats()
+        _lib.lib().gfs_sim_step_host(self._h, float(dt), _p(positions), _p(velocities), _p(ids), ctypes.byref(n),
+                                     ctypes.byref(st))
+        self.last_stats = st.as_dict()
+        return n.value, self.last_stats
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.lib().gfs_sim_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

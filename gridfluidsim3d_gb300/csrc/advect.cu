@@ -1,0 +1,325 @@
+// advect.cu -- grid -> particle: PIC/FLIP velocity update and RK advection.
+//
+// k_g2p_advect fuses stages 11 and 12 of FluidSimulation::_stepFluid
+// (fluidsimulation.cpp:3104-3209) for one particle per thread, in the
+// particles' (cell, id) order so that a warp touches a compact set of faces:
+//   vnew = tricubic(MAC, p), vold = tricubic(saved, p)
+//   v    = 0.05 vnew + 0.95 (v + vnew - vold)                (:3118-3128)
+//   p1   = RK4 through MAC (k1 = vnew: the same sample)       (particleadvector.cpp:1045-1054)
+//   if cell(p1) is solid: pull p1 back along p0->p1           (:3145-3179, collision.cpp:303-449)
+// The tricubic sample is MACVelocityField::evaluateVelocityAtPosition
+// (macvelocityfield.cpp:350-559): Catmull-Rom over a 4x4x4 stencil per
+// component, evaluated here in FP32 in separable form, reading the padded face
+// grids through the read-only path with no bounds checks (the zero halo is the
+// reference's out-of-range value).  With a power-of-two dx the stencil index
+// and the fractional offsets are formed exactly as the reference's doubles.
+#include "gfs_internal.h"
+
+namespace gfs {
+
+struct AdvArgs {
+    GridDim f[3], c;
+    float inv_dx;      // (float)(1/dx)
+    float bound[3];    // x < dx*n  <=>  x < bound (bound = smallest float >= dx*n)
+    double dx, inv_dx_d;
+    int pow2;
+    float h, f1, f6;   // RK4: (float)(0.5*dt), (float)dt, (float)(dt/6.0f)
+    float a_pic, b_flip;
+};
+
+__device__ __forceinline__ float interp_component(const float *__restrict__ g, const GridDim &f, float X,
+                                                  float Y, float Z) {
+    float fi = floorf(X), fj = floorf(Y), fk = floorf(Z);
+    int i = (int)fi, j = (int)fj, k = (int)fk;
+    float wx[4], wy[4], wz[4];
+    catmull_rom_weights(X - fi, wx);
+    catmull_rom_weights(Y - fj, wy);
+    catmull_rom_weights(Z - fk, wz);
+    const long long sy = f.sx, sz = (long long)f.sx * f.sy;
+    const float *base = g + f.at(i - 1, j - 1, k - 1);
+    float acc = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        float accb = 0.0f;
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const float *row = base + b * sy + c * sz;
+            float r = wx[0] * __ldg(row) + wx[1] * __ldg(row + 1) + wx[2] * __ldg(row + 2) + wx[3] * __ldg(row + 3);
+            accb += wy[b] * r;
+        }
+        acc += wz[c] * accb;
+    }
+    return acc;
+}
+
+// MACVelocityField::evaluateVelocityAtPosition: zero outside [0, n*dx).
+__device__ __forceinline__ float3 eval_velocity(const AdvArgs &A, const float *__restrict__ u,
+                                                const float *__restrict__ v, const float *__restrict__ w,
+                                                float x, float y, float z) {
+    if (!(x >= 0.f && y >= 0.f && z >= 0.f && x < A.bound[0] && y < A.bound[1] && z < A.bound[2]))
+        return make_float3(0.f, 0.f, 0.f);
+    float X, Y, Z;
+    if (A.pow2) {
+        X = x * A.inv_dx;
+        Y = y * A.inv_dx;
+        Z = z * A.inv_dx;
+    } else {
+        X = (float)((double)x * A.inv_dx_d);
+        Y = (float)((double)y * A.inv_dx_d);
+        Z = (float)((double)z * A.inv_dx_d);
+    }
+    // U samples at (i, j+1/2, k+1/2): shift y and z by half a cell, etc.
+    float vx = interp_component(u, A.f[0], X, Y - 0.5f, Z - 0.5f);
+    float vy = interp_component(v, A.f[1], X - 0.5f, Y, Z - 0.5f);
+    float vz = interp_component(w, A.f[2], X - 0.5f, Y - 0.5f, Z);
+    return make_float3(vx, vy, vz);
+}
+
+__device__ __forceinline__ bool finite3(float3 a) { return isfinite(a.x) && isfinite(a.y) && isfinite(a.z); }
+
+__device__ __forceinline__ void pos_cell(const AdvArgs &A, float x, float y, float z, int &i, int &j, int &k) {
+    if (A.pow2) {
+        i = (int)floorf(x * A.inv_dx);
+        j = (int)floorf(y * A.inv_dx);
+        k = (int)floorf(z * A.inv_dx);
+    } else {
+        i = (int)floor((double)x * A.inv_dx_d);
+        j = (int)floor((double)y * A.inv_dx_d);
+        k = (int)floor((double)z * A.inv_dx_d);
+    }
+}
+
+__device__ __forceinline__ bool cell_solid(const AdvArgs &A, const uint8_t *__restrict__ mat, int i, int j, int k) {
+    if (!A.c.in(i, j, k)) return true;   // out of range reads as solid
+    return mat[A.c.at(i, j, k)] == GFS_SOLID;
+}
+
+// Collision::getLineSegmentVoxelIntersection (collision.cpp:303-402)
+__device__ bool segment_voxel(const AdvArgs &A, const uint8_t *__restrict__ mat, float3 p0in, float3 p1in,
+                              int &vi, int &vj, int &vk) {
+    float s = (float)(1.0 / A.dx);
+    float p0x = __fmul_rn(p0in.x, s), p0y = __fmul_rn(p0in.y, s), p0z = __fmul_rn(p0in.z, s);
+    float p1x = __fmul_rn(p1in.x, s), p1y = __fmul_rn(p1in.y, s), p1z = __fmul_rn(p1in.z, s);
+    int gx0 = (int)floorf(p0x), gy0 = (int)floorf(p0y), gz0 = (int)floorf(p0z);
+    int gx1 = (int)floorf(p1x), gy1 = (int)floorf(p1y), gz1 = (int)floorf(p1z);
+    int sx = gx1 > gx0 ? 1 : gx1 < gx0 ? -1 : 0;
+    int sy = gy1 > gy0 ? 1 : gy1 < gy0 ? -1 : 0;
+    int sz = gz1 > gz0 ? 1 : gz1 < gz0 ? -1 : 0;
+    int gx = gx0, gy = gy0, gz = gz0;
+    double gxp = gx0 + (gx1 > gx0 ? 1 : 0), gyp = gy0 + (gy1 > gy0 ? 1 : 0), gzp = gz0 + (gz1 > gz0 ? 1 : 0);
+    double vx = p1x == p0x ? 1.0 : (double)__fsub_rn(p1x, p0x);
+    double vy = p1y == p0y ? 1.0 : (double)__fsub_rn(p1y, p0y);
+    double vz = p1z == p0z ? 1.0 : (double)__fsub_rn(p1z, p0z);
+    double vxvy = vx * vy, vxvz = vx * vz, vyvz = vy * vz;
+    double errx = (gxp - (double)p0x) * vyvz, erry = (gyp - (double)p0y) * vxvz, errz = (gzp - (double)p0z) * vxvy;
+    double derrx = sx * vyvz, derry = sy * vxvz, derrz = sz * vxvy;
+    int limit = abs(gx1 - gx0) + abs(gy1 - gy0) + abs(gz1 - gz0) + 3;
+    for (int it = 0; it < limit; it++) {
+        if (A.c.in(gx, gy, gz) && mat[A.c.at(gx, gy, gz)] == GFS_SOLID) {
+            vi = gx; vj = gy; vk = gz;
+            return true;
+        }
+        if (gx == gx1 && gy == gy1 && gz == gz1) break;
+        double xr = fabs(errx), yr = fabs(erry), zr = fabs(errz);
+        if (sx != 0 && (sy == 0 || xr < yr) && (sz == 0 || xr < zr)) { gx += sx; errx += derrx; }
+        else if (sy != 0 && (sz == 0 || yr < zr)) { gy += sy; erry += derry; }
+        else if (sz != 0) { gz += sz; errz += derrz; }
+    }
+    return false;
+}
+
+// FluidSimulation::_resolveParticleSolidCellCollision (fluidsimulation.cpp:3145-3179)
+// with Collision::rayIntersectsAABB (collision.cpp:404-449, including its use of
+// dir.x to guard dir.z).
+__device__ float3 resolve_collision(const AdvArgs &A, const uint8_t *__restrict__ mat, float3 p0, float3 p1) {
+    int vi, vj, vk;
+    if (!segment_voxel(A, mat, p0, p1, vi, vj, vk)) return p0;
+    float dxr = __fsub_rn(p1.x, p0.x), dyr = __fsub_rn(p1.y, p0.y), dzr = __fsub_rn(p1.z, p0.z);
+    float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dxr, dxr), __fmul_rn(dyr, dyr)), __fmul_rn(dzr, dzr)));
+    float linv = (float)(1.0 / (double)len);
+    float3 rn = make_float3(__fmul_rn(dxr, linv), __fmul_rn(dyr, linv), __fmul_rn(dzr, linv));
+    float bmin[3], bmax[3];
+    int vv[3] = {vi, vj, vk};
+    for (int q = 0; q < 3; q++) {
+        bmin[q] = (float)((double)(float)vv[q] * A.dx);
+        bmax[q] = __fadd_rn(bmin[q], (float)A.dx);
+    }
+    float dir[3] = {rn.x, rn.y, rn.z};
+    const double eps = 1e-10;
+    if (fabs((double)dir[0]) < eps) dir[0] = dir[0] < 0 ? (float)-eps : (float)eps;
+    if (fabs((double)dir[1]) < eps) dir[1] = dir[1] < 0 ? (float)-eps : (float)eps;
+    if (fabs((double)dir[0]) < eps) dir[2] = dir[2] < 0 ? (float)-eps : (float)eps;
+    float inv[3] = {(float)(1.0 / (double)dir[0]), (float)(1.0 / (double)dir[1]), (float)(1.0 / (double)dir[2])};
+    float p0a[3] = {p0.x, p0.y, p0.z};
+    double tmin = 0, tmax = 0;
+    for (int q = 0; q < 3; q++) {
+        double t1 = (double)__fmul_rn(__fsub_rn(bmin[q], p0a[q]), inv[q]);
+        double t2 = (double)__fmul_rn(__fsub_rn(bmax[q], p0a[q]), inv[q]);
+        if (q == 0) { tmin = fmin(t1, t2); tmax = fmax(t1, t2); }
+        else { tmin = fmax(tmin, fmin(t1, t2)); tmax = fmin(tmax, fmax(t1, t2)); }
+    }
+    if (!(tmax > fmax(tmin, 0.0))) return p0;
+    float ft = (float)tmin;
+    float cp[3];
+    for (int q = 0; q < 3; q++) cp[q] = __fadd_rn(p0a[q], __fmul_rn(ft, dir[q]));
+    float back = (float)(0.05 * A.dx);
+    float3 res = make_float3(__fsub_rn(cp[0], __fmul_rn(back, rn.x)), __fsub_rn(cp[1], __fmul_rn(back, rn.y)),
+                             __fsub_rn(cp[2], __fmul_rn(back, rn.z)));
+    int ri, rj, rk;
+    pos_cell(A, res.x, res.y, res.z, ri, rj, rk);
+    if (cell_solid(A, mat, ri, rj, rk)) return p0;
+    return res;
+}
+
+__device__ __forceinline__ float3 axpy3(float3 p, float h, float3 k) {
+    return make_float3(__fadd_rn(p.x, __fmul_rn(h, k.x)), __fadd_rn(p.y, __fmul_rn(h, k.y)),
+                       __fadd_rn(p.z, __fmul_rn(h, k.z)));
+}
+
+// p0 + f6 * (k1 + 2 k2 + 2 k3 + k4), float, left to right (particleadvector.cpp:1051)
+__device__ __forceinline__ float rk4_comb(float p, float f6, float k1, float k2, float k3, float k4) {
+    float sum = __fadd_rn(__fadd_rn(__fadd_rn(k1, __fmul_rn(2.0f, k2)), __fmul_rn(2.0f, k3)), k4);
+    return __fadd_rn(p, __fmul_rn(f6, sum));
+}
+
+__global__ void __launch_bounds__(128) k_g2p_advect(AdvArgs A, float4 *__restrict__ pos, float4 *__restrict__ vel,
+                                                    const uint32_t *__restrict__ num, long long nbound,
+                                                    const float *__restrict__ mu, const float *__restrict__ mv,
+                                                    const float *__restrict__ mw, const float *__restrict__ su,
+                                                    const float *__restrict__ sv, const float *__restrict__ sw,
+                                                    const uint8_t *__restrict__ mat) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= nbound || p >= (long long)num[0]) return;
+    float4 P = pos[p];
+    float4 V = vel[p];
+    float3 vnew = eval_velocity(A, mu, mv, mw, P.x, P.y, P.z);
+    float3 vold = eval_velocity(A, su, sv, sw, P.x, P.y, P.z);
+    // ParticleAdvector::_validateOutput on both samples (particleadvector.cpp:1139-1149)
+    float3 vn = finite3(vnew) ? vnew : make_float3(0.f, 0.f, 0.f);
+    float3 vo = finite3(vold) ? vold : make_float3(0.f, 0.f, 0.f);
+    float4 Vn;
+    Vn.x = __fadd_rn(__fmul_rn(A.a_pic, vn.x), __fmul_rn(A.b_flip, __fsub_rn(__fadd_rn(V.x, vn.x), vo.x)));
+    Vn.y = __fadd_rn(__fmul_rn(A.a_pic, vn.y), __fmul_rn(A.b_flip, __fsub_rn(__fadd_rn(V.y, vn.y), vo.y)));
+    Vn.z = __fadd_rn(__fmul_rn(A.a_pic, vn.z), __fmul_rn(A.b_flip, __fsub_rn(__fadd_rn(V.z, vn.z), vo.z)));
+    Vn.w = 0.f;
+    // RK4 through the MAC field; k1 is the vnew sample
+    float3 p0 = make_float3(P.x, P.y, P.z);
+    float3 k1 = vnew;
+    float3 t = axpy3(p0, A.h, k1);
+    float3 k2 = eval_velocity(A, mu, mv, mw, t.x, t.y, t.z);
+    t = axpy3(p0, A.h, k2);
+    float3 k3 = eval_velocity(A, mu, mv, mw, t.x, t.y, t.z);
+    t = axpy3(p0, A.f1, k3);
+    float3 k4 = eval_velocity(A, mu, mv, mw, t.x, t.y, t.z);
+    float3 p1 = make_float3(rk4_comb(p0.x, A.f6, k1.x, k2.x, k3.x, k4.x),
+                            rk4_comb(p0.y, A.f6, k1.y, k2.y, k3.y, k4.y),
+                            rk4_comb(p0.z, A.f6, k1.z, k2.z, k3.z, k4.z));
+    int ci, cj, ck;
+    pos_cell(A, p1.x, p1.y, p1.z, ci, cj, ck);
+    if (!(isfinite(p1.x) && isfinite(p1.y) && isfinite(p1.z)) || cell_solid(A, mat, ci, cj, ck))
+        p1 = resolve_collision(A, mat, p0, p1);
+    pos[p] = make_float4(p1.x, p1.y, p1.z, P.w);
+    vel[p] = Vn;
+}
+
+static float float_ceil_of(double x) {
+    float f = (float)x;
+    if ((double)f < x) f = nextafterf(f, INFINITY);
+    return f;
+}
+
+static AdvArgs make_adv(const Grids &g, double dt, double ratio_pic) {
+    AdvArgs A;
+    for (int d = 0; d < 3; d++) A.f[d] = g.f[d];
+    A.c = g.c;
+    A.dx = g.dx;
+    A.inv_dx_d = 1.0 / g.dx;
+    A.inv_dx = (float)(1.0 / g.dx);
+    int e;
+    double m = frexp(g.dx, &e);
+    A.pow2 = (m == 0.5) ? 1 : 0;
+    A.bound[0] = float_ceil_of(g.dx * g.ni);
+    A.bound[1] = float_ceil_of(g.dx * g.nj);
+    A.bound[2] = float_ceil_of(g.dx * g.nk);
+    A.h = (float)(0.5 * dt);
+    A.f1 = (float)dt;
+    A.f6 = (float)(dt / 6.0f);
+    A.a_pic = (float)ratio_pic;
+    A.b_flip = (float)(1 - ratio_pic);
+    return A;
+}
+
+int g2p_advect(Sim *s, double dt) {
+    Ctx *ctx = s->ctx;
+    AdvArgs A = make_adv(s->g, dt, s->params.ratio_pic);
+    long long nb = s->n_bound;
+    if (nb == 0) return GFS_OK;
+    k_g2p_advect<<<grid_blocks(nb, 128), 128, 0, ctx->stream>>>(
+        A, s->pos.as<float4>(), s->vel.as<float4>(), s->num.as<uint32_t>(), nb, s->mac[0].as<float>(),
+        s->mac[1].as<float>(), s->mac[2].as<float>(), s->saved[0].as<float>(), s->saved[1].as<float>(),
+        s->saved[2].as<float>(), s->mat.as<uint8_t>());
+    ctx->launches++;
+    GFS_LAUNCH_CHECK();
+    return GFS_OK;
+}
+
+// -------------------------------------------- standalone point evaluation
+
+// order 0: tricubic sample (validated); 1..4: RK of that order
+// (ParticleAdvector::_RK1.._RK4, particleadvector.cpp:1045-1078).
+__global__ void __launch_bounds__(128) k_points(AdvArgs A, const float *__restrict__ pts, long long n,
+                                                const float *__restrict__ u, const float *__restrict__ v,
+                                                const float *__restrict__ w, float *__restrict__ out, int order,
+                                                int validate, float dtf, float h05, float h075, float f9) {
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    float3 p0 = make_float3(pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]);
+    float3 r;
+    float3 k1 = eval_velocity(A, u, v, w, p0.x, p0.y, p0.z);
+    if (order == 0) {
+        r = (validate && !finite3(k1)) ? make_float3(0.f, 0.f, 0.f) : k1;
+    } else if (order == 1) {
+        r = axpy3(p0, dtf, k1);
+    } else if (order == 2) {
+        float3 t = axpy3(p0, h05, k1);
+        float3 k2 = eval_velocity(A, u, v, w, t.x, t.y, t.z);
+        r = axpy3(p0, dtf, k2);
+    } else if (order == 3) {
+        float3 t = axpy3(p0, h05, k1);
+        float3 k2 = eval_velocity(A, u, v, w, t.x, t.y, t.z);
+        t = axpy3(p0, h075, k2);
+        float3 k3 = eval_velocity(A, u, v, w, t.x, t.y, t.z);
+        // p0 + (float)(dt/9.0f)*(2k1 + 3k2 + 4k3)
+        float sx = __fadd_rn(__fadd_rn(__fmul_rn(2.f, k1.x), __fmul_rn(3.f, k2.x)), __fmul_rn(4.f, k3.x));
+        float sy = __fadd_rn(__fadd_rn(__fmul_rn(2.f, k1.y), __fmul_rn(3.f, k2.y)), __fmul_rn(4.f, k3.y));
+        float sz = __fadd_rn(__fadd_rn(__fmul_rn(2.f, k1.z), __fmul_rn(3.f, k2.z)), __fmul_rn(4.f, k3.z));
+        r = make_float3(__fadd_rn(p0.x, __fmul_rn(f9, sx)), __fadd_rn(p0.y, __fmul_rn(f9, sy)),
+                        __fadd_rn(p0.z, __fmul_rn(f9, sz)));
+    } else {
+        float3 t = axpy3(p0, A.h, k1);
+        float3 k2 = eval_velocity(A, u, v, w, t.x, t.y, t.z);
+        t = axpy3(p0, A.h, k2);
+        float3 k3 = eval_velocity(A, u, v, w, t.x, t.y, t.z);
+        t = axpy3(p0, A.f1, k3);
+        float3 k4 = eval_velocity(A, u, v, w, t.x, t.y, t.z);
+        r = make_float3(rk4_comb(p0.x, A.f6, k1.x, k2.x, k3.x, k4.x), rk4_comb(p0.y, A.f6, k1.y, k2.y, k3.y, k4.y),
+                        rk4_comb(p0.z, A.f6, k1.z, k2.z, k3.z, k4.z));
+    }
+    out[3 * q] = r.x;
+    out[3 * q + 1] = r.y;
+    out[3 * q + 2] = r.z;
+}
+
+int interpolate_points(Ctx *ctx, const Grids &g, float *const mac[3], const float *d_points, int64_t n,
+                       float *d_out, int rk_order, double dt, bool validate) {
+    if (n == 0) return GFS_OK;
+    AdvArgs A = make_adv(g, dt, 0.0);
+    k_points<<<grid_blocks(n, 128), 128, 0, ctx->stream>>>(A, d_points, n, mac[0], mac[1], mac[2], d_out, rk_order,
+                                                           validate ? 1 : 0, (float)dt, (float)(0.5 * dt),
+                                                           (float)(0.75 * dt), (float)(dt / 9.0f));
+    ctx->launches++;
+    GFS_LAUNCH_CHECK();
+    return GFS_OK;
+}
+
+}  // namespace gfs

@@ -1,0 +1,681 @@
+// capi.cu -- the extern "C" boundary of libgfs (declared in include/gfs.h).
+//
+// Status codes plus a thread-local error string replace the reference's
+// c_bindings convention (int *err + CBINDINGS_ERROR_MESSAGE, cbindings.h:20-135);
+// no exception crosses the ABI.  Host buffers are borrowed for the duration of a
+// call.  Standalone entry points (splat, interpolate, advect, pressure) stage the
+// caller's arrays into padded device grids, run the same kernels the
+// device-resident substep runs, and copy the result back.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "gfs_internal.h"
+
+namespace gfs {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(int code, const char *fmt, ...) {
+    (void)code;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int DevMem::alloc(size_t n) {
+    release();
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        set_error(GFS_ERR_NOMEM, "cudaMalloc(%zu bytes) failed: %s", n, cudaGetErrorString(e));
+        return GFS_ERR_NOMEM;
+    }
+    bytes = n;
+    return GFS_OK;
+}
+
+int DevMem::ensure(size_t n) {
+    if (p && bytes >= n) return GFS_OK;
+    return alloc(n);
+}
+
+void DevMem::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+// ------------------------------------------------- padded <-> flat grids
+
+template <class T>
+__global__ void k_pad(const T *__restrict__ src, GridDim g, T *__restrict__ dst) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y, k = blockIdx.z;
+    if (i >= g.nx) return;
+    dst[g.at(i, j, k)] = src[i + (long long)g.nx * (j + (long long)g.ny * k)];
+}
+
+template <class T>
+__global__ void k_unpad(const T *__restrict__ src, GridDim g, T *__restrict__ dst) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y, k = blockIdx.z;
+    if (i >= g.nx) return;
+    dst[i + (long long)g.nx * (j + (long long)g.ny * k)] = src[g.at(i, j, k)];
+}
+
+// host flat -> device padded (through a device staging buffer)
+template <class T>
+static int upload_padded(Ctx *ctx, const T *h, const GridDim &g, T *d_padded, DevMem &stage) {
+    size_t n = (size_t)g.nx * g.ny * g.nz;
+    if (stage.ensure(n * sizeof(T))) return GFS_ERR_NOMEM;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(stage.p, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    dim3 grid(grid_blocks(g.nx, 128), g.ny, g.nz);
+    k_pad<T><<<grid, 128, 0, ctx->stream>>>(stage.as<T>(), g, d_padded);
+    ctx->launches++;
+    GFS_LAUNCH_CHECK();
+    return GFS_OK;
+}
+
+template <class T>
+static int download_padded(Ctx *ctx, const T *d_padded, const GridDim &g, T *h, DevMem &stage) {
+    size_t n = (size_t)g.nx * g.ny * g.nz;
+    if (stage.ensure(n * sizeof(T))) return GFS_ERR_NOMEM;
+    dim3 grid(grid_blocks(g.nx, 128), g.ny, g.nz);
+    k_unpad<T><<<grid, 128, 0, ctx->stream>>>(d_padded, g, stage.as<T>());
+    ctx->launches++;
+    GFS_LAUNCH_CHECK();
+    GFS_CUDA_CHECK(cudaMemcpyAsync(h, stage.p, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+    GFS_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    return GFS_OK;
+}
+
+// ------------------------------------------------------ particle packing
+
+__global__ void k_pack_particles(const float *__restrict__ p3, const float *__restrict__ v3,
+                                 const uint32_t *__restrict__ ids, long long n, float4 *__restrict__ pos,
+                                 float4 *__restrict__ vel) {
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    uint32_t id = ids ? ids[q] : (uint32_t)q;
+    pos[q] = make_float4(p3[3 * q], p3[3 * q + 1], p3[3 * q + 2], __uint_as_float(id));
+    vel[q] = v3 ? make_float4(v3[3 * q], v3[3 * q + 1], v3[3 * q + 2], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void k_unpack_particles(const float4 *__restrict__ pos, const float4 *__restrict__ vel, long long n,
+                                   float *__restrict__ p3, float *__restrict__ v3, uint32_t *__restrict__ ids) {
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    float4 p = pos[q], v = vel[q];
+    p3[3 * q] = p.x; p3[3 * q + 1] = p.y; p3[3 * q + 2] = p.z;
+    v3[3 * q] = v.x; v3[3 * q + 1] = v.y; v3[3 * q + 2] = v.z;
+    ids[q] = __float_as_uint(p.w);
+}
+
+static bool valid_dims(int ni, int nj, int nk) {
+    return ni > 0 && nj > 0 && nk > 0 && (long long)ni * nj * nk < (1LL << 31);
+}
+
+// -------------------------------------------------------------- sim core
+
+static int sim_init(Sim *s, Ctx *ctx, int ni, int nj, int nk, double dx, int64_t cap) {
+    s->ctx = ctx;
+    s->g = make_grids(ni, nj, nk, dx);
+    gfs_sim_default_params(&s->params);
+    s->capacity = cap;
+    int e;
+    double m = frexp(dx, &e);
+    s->dx_pow2 = (m == 0.5);
+    s->inv_dx_f = (float)(1.0 / dx);
+    cudaStream_t st = ctx->stream;
+    const GridDim &c = s->g.c;
+    long long ncells = (long long)ni * nj * nk;
+    int rc = 0;
+    rc |= s->mat.alloc((size_t)c.size);
+    rc |= s->layer.alloc((size_t)c.size);
+    for (int d = 0; d < 3; d++) {
+        const GridDim &f = s->g.f[d];
+        rc |= s->mac[d].alloc((size_t)f.size * sizeof(float));
+        rc |= s->saved[d].alloc((size_t)f.size * sizeof(float));
+        rc |= s->sval[d].alloc((size_t)f.size * sizeof(float));
+        rc |= s->smask[d].alloc((size_t)f.size);
+    }
+    size_t pc = (size_t)std::max<int64_t>(cap, 1);
+    rc |= s->pos.alloc(pc * sizeof(float4));
+    rc |= s->vel.alloc(pc * sizeof(float4));
+    rc |= s->pos_alt.alloc(pc * sizeof(float4));
+    rc |= s->vel_alt.alloc(pc * sizeof(float4));
+    rc |= s->key.alloc(pc * sizeof(uint32_t));
+    rc |= s->slot.alloc(pc * sizeof(uint32_t));
+    rc |= s->count.alloc((size_t)(ncells + 1) * sizeof(uint32_t));
+    rc |= s->offset.alloc((size_t)(ncells + 1) * sizeof(uint32_t));
+    rc |= s->scan_tmp.alloc(scan_temp_elems(ncells + 1) * sizeof(uint32_t));
+    rc |= s->num.alloc(4 * sizeof(uint32_t));
+    if (rc) return GFS_ERR_NOMEM;
+    GFS_CUDA_CHECK(cudaMemsetAsync(s->mat.p, GFS_SOLID, s->mat.bytes, st));
+    GFS_CUDA_CHECK(cudaMemsetAsync(s->layer.p, 0xFF, s->layer.bytes, st));
+    for (int d = 0; d < 3; d++) {
+        GFS_CUDA_CHECK(cudaMemsetAsync(s->mac[d].p, 0, s->mac[d].bytes, st));
+        GFS_CUDA_CHECK(cudaMemsetAsync(s->saved[d].p, 0, s->saved[d].bytes, st));
+        GFS_CUDA_CHECK(cudaMemsetAsync(s->sval[d].p, 0, s->sval[d].bytes, st));
+        GFS_CUDA_CHECK(cudaMemsetAsync(s->smask[d].p, 0, s->smask[d].bytes, st));
+    }
+    GFS_CUDA_CHECK(cudaMemsetAsync(s->num.p, 0, s->num.bytes, st));
+    GFS_CUDA_CHECK(cudaMemsetAsync(s->offset.p, 0, s->offset.bytes, st));
+    // interior of the material grid: air
+    DevMem stage;
+    std::vector<uint8_t> air((size_t)ncells, GFS_AIR);
+    rc = upload_padded<uint8_t>(ctx, air.data(), c, s->mat.as<uint8_t>(), stage);
+    if (rc) return rc;
+    GFS_CUDA_CHECK(cudaStreamSynchronize(st));
+    GFS_CUDA_CHECK(cudaEventCreate(&s->ev0));
+    GFS_CUDA_CHECK(cudaEventCreate(&s->ev1));
+    GFS_CUDA_CHECK(cudaEventCreate(&s->evp0));
+    GFS_CUDA_CHECK(cudaEventCreate(&s->evp1));
+    return GFS_OK;
+}
+
+static int sim_set_particles(Sim *s, const float *hp, const float *hv, const uint32_t *hid, int64_t n) {
+    Ctx *ctx = s->ctx;
+    if (n < 0 || n > s->capacity) {
+        set_error(GFS_ERR_INVALID, "particle count %lld outside [0, capacity %lld]", (long long)n,
+                  (long long)s->capacity);
+        return GFS_ERR_INVALID;
+    }
+    if (n > 0 && !hp) {
+        set_error(GFS_ERR_INVALID, "positions pointer is NULL");
+        return GFS_ERR_INVALID;
+    }
+    cudaStream_t st = ctx->stream;
+    // stage xyz triples in the alternate buffers (16 B per particle >= 12 B)
+    float *p3 = s->pos_alt.as<float>(), *v3 = s->vel_alt.as<float>();
+    uint32_t *ids = s->key.as<uint32_t>();
+    if (n > 0) {
+        GFS_CUDA_CHECK(cudaMemcpyAsync(p3, hp, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, st));
+        if (hv) GFS_CUDA_CHECK(cudaMemcpyAsync(v3, hv, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, st));
+        if (hid) GFS_CUDA_CHECK(cudaMemcpyAsync(ids, hid, (size_t)n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        k_pack_particles<<<grid_blocks(n, 256), 256, 0, st>>>(p3, hv ? v3 : nullptr, hid ? ids : nullptr, n,
+                                                              s->pos.as<float4>(), s->vel.as<float4>());
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+    }
+    uint32_t hn = (uint32_t)n;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(s->num.p, &hn, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    s->n_bound = n;
+    s->need_sort = true;
+    return GFS_OK;
+}
+
+static int sim_get_particles(Sim *s, float *hp, float *hv, uint32_t *hid, int64_t *n_out) {
+    Ctx *ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    uint32_t hn = 0;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(&hn, s->num.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GFS_CUDA_CHECK(cudaStreamSynchronize(st));
+    long long n = hn;
+    if (n_out) *n_out = n;
+    if (n > 0 && (hp || hv || hid)) {
+        float *p3 = s->pos_alt.as<float>(), *v3 = s->vel_alt.as<float>();
+        uint32_t *ids = s->key.as<uint32_t>();
+        k_unpack_particles<<<grid_blocks(n, 256), 256, 0, st>>>(s->pos.as<float4>(), s->vel.as<float4>(), n, p3,
+                                                                v3, ids);
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+        if (hp) GFS_CUDA_CHECK(cudaMemcpyAsync(hp, p3, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (hv) GFS_CUDA_CHECK(cudaMemcpyAsync(hv, v3, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (hid) GFS_CUDA_CHECK(cudaMemcpyAsync(hid, ids, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        GFS_CUDA_CHECK(cudaStreamSynchronize(st));
+    }
+    return GFS_OK;
+}
+
+static int sim_step(Sim *s, double dt, gfs_step_stats *stats) {
+    Ctx *ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    if (!(dt >= 0.0) || !std::isfinite(dt)) {
+        set_error(GFS_ERR_INVALID, "delta time must be >= 0 (got %g)", dt);
+        return GFS_ERR_INVALID;
+    }
+    GFS_CUDA_CHECK(cudaEventRecord(s->ev0, st));
+    int rc = GFS_OK;
+    // stage 1: _updateFluidCells (particle removal happened in the last sort)
+    if (s->need_sort && (rc = sort_particles(s, true))) return rc;
+    if ((rc = classify_cells(s))) return rc;
+    // stage 5: velocity splat, fill, saved field, body forces (stage 6 fused)
+    if ((rc = splat_velocity(s))) return rc;
+    if ((rc = face_fill(s, dt))) return rc;
+    int layers = (int)std::ceil(s->params.cfl + 2.0);
+    if (layers > 120) layers = 120;
+    if ((rc = build_layers(s, layers))) return rc;
+    float *saved[3] = {s->saved[0].as<float>(), s->saved[1].as<float>(), s->saved[2].as<float>()};
+    if ((rc = extrapolate_field(s, saved, layers, false))) return rc;
+    // stage 7: pressure
+    GFS_CUDA_CHECK(cudaEventRecord(s->evp0, st));
+    float *mac[3] = {s->mac[0].as<float>(), s->mac[1].as<float>(), s->mac[2].as<float>()};
+    gfs_step_stats local{};
+    rc = pressure_solve(ctx, s->ps, s->g, s->mat.as<uint8_t>(), mac, s->params.density, dt, s->params.precision,
+                        s->params.tol, s->params.max_cg_iterations, &local);
+    if (rc) return rc;
+    GFS_CUDA_CHECK(cudaEventRecord(s->evp1, st));
+    // stage 8, 9
+    if ((rc = pressure_apply(s, dt))) return rc;
+    if ((rc = extrapolate_field(s, mac, layers, false))) return rc;
+    // stages 11, 12
+    if ((rc = g2p_advect(s, dt))) return rc;
+    if ((rc = sort_particles(s, true))) return rc;
+    GFS_CUDA_CHECK(cudaEventRecord(s->ev1, st));
+    GFS_CUDA_CHECK(cudaEventSynchronize(s->ev1));
+    uint32_t hnum[4];
+    GFS_CUDA_CHECK(cudaMemcpy(hnum, s->num.p, sizeof(hnum), cudaMemcpyDeviceToHost));
+    float ms = 0.f, pms = 0.f;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    cudaEventElapsedTime(&pms, s->evp0, s->evp1);
+    local.num_particles = hnum[0];
+    local.num_fluid_cells = hnum[2];
+    local.step_ms = ms;
+    local.pressure_ms = pms;
+    s->last = local;
+    if (stats) *stats = local;
+    return GFS_OK;
+}
+
+}  // namespace gfs
+
+using namespace gfs;
+
+#define GFS_NONNULL(ptr)                                           \
+    do {                                                           \
+        if (!(ptr)) {                                              \
+            set_error(GFS_ERR_INVALID, "%s must not be NULL", #ptr); \
+            return GFS_ERR_INVALID;                                \
+        }                                                          \
+    } while (0)
+
+extern "C" {
+
+const char *gfs_last_error(void) { return g_err; }
+
+const char *gfs_version(void) { return "gfs-gb300 0.1 (sm_103a)"; }
+
+int gfs_ctx_create(int device, gfs_ctx **out) {
+    GFS_NONNULL(out);
+    *out = nullptr;
+    int ndev = 0;
+    GFS_CUDA_CHECK(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) {
+        set_error(GFS_ERR_INVALID, "device %d out of range (%d devices)", device, ndev);
+        return GFS_ERR_INVALID;
+    }
+    GFS_CUDA_CHECK(cudaSetDevice(device));
+    gfs_ctx *c = new (std::nothrow) gfs_ctx();
+    if (!c) {
+        set_error(GFS_ERR_NOMEM, "host allocation failed");
+        return GFS_ERR_NOMEM;
+    }
+    c->c.device = device;
+    cudaDeviceProp prop;
+    cudaError_t e = cudaGetDeviceProperties(&prop, device);
+    if (e == cudaSuccess) {
+        c->c.num_sms = prop.multiProcessorCount;
+        snprintf(c->c.device_name, sizeof(c->c.device_name), "%s", prop.name);
+    }
+    e = cudaStreamCreateWithFlags(&c->c.stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        set_error(GFS_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+        delete c;
+        return GFS_ERR_CUDA;
+    }
+    *out = c;
+    return GFS_OK;
+}
+
+int gfs_ctx_destroy(gfs_ctx *ctx) {
+    if (!ctx) return GFS_OK;
+    cudaSetDevice(ctx->c.device);
+    cudaStreamSynchronize(ctx->c.stream);
+    cudaStreamDestroy(ctx->c.stream);
+    delete ctx;
+    return GFS_OK;
+}
+
+int gfs_ctx_synchronize(gfs_ctx *ctx) {
+    GFS_NONNULL(ctx);
+    GFS_CUDA_CHECK(cudaStreamSynchronize(ctx->c.stream));
+    return GFS_OK;
+}
+
+int gfs_ctx_stream(gfs_ctx *ctx, void **stream) {
+    GFS_NONNULL(ctx);
+    GFS_NONNULL(stream);
+    *stream = (void *)ctx->c.stream;
+    return GFS_OK;
+}
+
+int gfs_ctx_device_name(gfs_ctx *ctx, char *buf, int buflen) {
+    GFS_NONNULL(ctx);
+    GFS_NONNULL(buf);
+    snprintf(buf, (size_t)std::max(buflen, 1), "%s", ctx->c.device_name);
+    return GFS_OK;
+}
+
+int gfs_ctx_launch_count(gfs_ctx *ctx, int64_t *count) {
+    GFS_NONNULL(ctx);
+    GFS_NONNULL(count);
+    *count = ctx->c.launches;
+    return GFS_OK;
+}
+
+int gfs_sim_default_params(gfs_sim_params *p) {
+    GFS_NONNULL(p);
+    p->density = 20.0;
+    p->ratio_pic = (double)0.05f;
+    p->cfl = 5.0;
+    p->gravity[0] = 0.0f;
+    p->gravity[1] = -25.0f;
+    p->gravity[2] = 0.0f;
+    p->max_particles_per_cell = 100;
+    p->precision = GFS_PRECISION_PLAIN;
+    p->tol = 1e-6;
+    p->max_cg_iterations = 200;
+    return GFS_OK;
+}
+
+int gfs_sim_create(gfs_ctx *ctx, int ni, int nj, int nk, double dx, int64_t max_particles, gfs_sim **out) {
+    GFS_NONNULL(ctx);
+    GFS_NONNULL(out);
+    *out = nullptr;
+    if (!valid_dims(ni, nj, nk) || !(dx > 0.0) || max_particles < 0 || max_particles > 0xFFFFFFF0LL) {
+        set_error(GFS_ERR_INVALID, "invalid simulation size %d x %d x %d, dx %g, %lld particles", ni, nj, nk, dx,
+                  (long long)max_particles);
+        return GFS_ERR_INVALID;
+    }
+    GFS_CUDA_CHECK(cudaSetDevice(ctx->c.device));
+    gfs_sim *s = new (std::nothrow) gfs_sim();
+    if (!s) {
+        set_error(GFS_ERR_NOMEM, "host allocation failed");
+        return GFS_ERR_NOMEM;
+    }
+    int rc = sim_init(&s->s, &ctx->c, ni, nj, nk, dx, max_particles);
+    if (rc) {
+        gfs_sim_destroy(s);
+        return rc;
+    }
+    *out = s;
+    return GFS_OK;
+}
+
+int gfs_sim_destroy(gfs_sim *sim) {
+    if (!sim) return GFS_OK;
+    Sim *s = &sim->s;
+    if (s->ctx) cudaStreamSynchronize(s->ctx->stream);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->evp0) cudaEventDestroy(s->evp0);
+    if (s->evp1) cudaEventDestroy(s->evp1);
+    delete sim;
+    return GFS_OK;
+}
+
+int gfs_sim_set_params(gfs_sim *sim, const gfs_sim_params *p) {
+    GFS_NONNULL(sim);
+    GFS_NONNULL(p);
+    if (!(p->density > 0) || !(p->cfl >= 0) || p->max_cg_iterations < 0 ||
+        (p->precision != GFS_PRECISION_PLAIN && p->precision != GFS_PRECISION_MIXED)) {
+        set_error(GFS_ERR_INVALID, "invalid simulation parameters");
+        return GFS_ERR_INVALID;
+    }
+    sim->s.params = *p;
+    if (sim->s.params.tol <= 0) sim->s.params.tol = 1e-6;
+    return GFS_OK;
+}
+
+int gfs_sim_get_params(gfs_sim *sim, gfs_sim_params *p) {
+    GFS_NONNULL(sim);
+    GFS_NONNULL(p);
+    *p = sim->s.params;
+    return GFS_OK;
+}
+
+int gfs_sim_set_material(gfs_sim *sim, const uint8_t *h_material) {
+    GFS_NONNULL(sim);
+    GFS_NONNULL(h_material);
+    Sim *s = &sim->s;
+    DevMem stage;
+    int rc = upload_padded<uint8_t>(s->ctx, h_material, s->g.c, s->mat.as<uint8_t>(), stage);
+    if (rc) return rc;
+    GFS_CUDA_CHECK(cudaStreamSynchronize(s->ctx->stream));
+    s->need_sort = true;   // particles in new solid cells go at the next step
+    return GFS_OK;
+}
+
+int gfs_sim_get_material(gfs_sim *sim, uint8_t *h_material) {
+    GFS_NONNULL(sim);
+    GFS_NONNULL(h_material);
+    DevMem stage;
+    return download_padded<uint8_t>(sim->s.ctx, sim->s.mat.as<uint8_t>(), sim->s.g.c, h_material, stage);
+}
+
+int gfs_sim_set_particles(gfs_sim *sim, const float *h_positions, const float *h_velocities,
+                          const uint32_t *h_ids, int64_t n) {
+    GFS_NONNULL(sim);
+    int rc = sim_set_particles(&sim->s, h_positions, h_velocities, h_ids, n);
+    if (rc) return rc;
+    return sort_particles(&sim->s, true);
+}
+
+int gfs_sim_num_particles(gfs_sim *sim, int64_t *n) {
+    GFS_NONNULL(sim);
+    GFS_NONNULL(n);
+    return sim_get_particles(&sim->s, nullptr, nullptr, nullptr, n);
+}
+
+int gfs_sim_get_particles(gfs_sim *sim, float *h_positions, float *h_velocities, uint32_t *h_ids, int64_t *n) {
+    GFS_NONNULL(sim);
+    return sim_get_particles(&sim->s, h_positions, h_velocities, h_ids, n);
+}
+
+int gfs_sim_get_velocity_field(gfs_sim *sim, float *h_u, float *h_v, float *h_w) {
+    GFS_NONNULL(sim);
+    Sim *s = &sim->s;
+    float *h[3] = {h_u, h_v, h_w};
+    DevMem stage;
+    for (int d = 0; d < 3; d++) {
+        if (!h[d]) continue;
+        int rc = download_padded<float>(s->ctx, s->mac[d].as<float>(), s->g.f[d], h[d], stage);
+        if (rc) return rc;
+    }
+    return GFS_OK;
+}
+
+int gfs_sim_get_pressure_grid(gfs_sim *sim, float *h_pressure) {
+    GFS_NONNULL(sim);
+    GFS_NONNULL(h_pressure);
+    Sim *s = &sim->s;
+    if (s->ps.allocated_for < 0) {
+        memset(h_pressure, 0, sizeof(float) * (size_t)s->g.ni * s->g.nj * s->g.nk);
+        return GFS_OK;
+    }
+    size_t n = (size_t)s->g.ni * s->g.nj * s->g.nk;
+    if (s->pgrid.ensure(n * sizeof(float))) return GFS_ERR_NOMEM;
+    int rc = pressure_to_grid(s->ctx, s->ps, s->g, s->pgrid.as<float>());
+    if (rc) return rc;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(h_pressure, s->pgrid.p, n * sizeof(float), cudaMemcpyDeviceToHost, s->ctx->stream));
+    GFS_CUDA_CHECK(cudaStreamSynchronize(s->ctx->stream));
+    return GFS_OK;
+}
+
+int gfs_sim_step(gfs_sim *sim, double dt, gfs_step_stats *stats) {
+    GFS_NONNULL(sim);
+    return sim_step(&sim->s, dt, stats);
+}
+
+int gfs_sim_step_host(gfs_sim *sim, double dt, float *h_positions, float *h_velocities, uint32_t *h_ids,
+                      int64_t *n, gfs_step_stats *stats) {
+    GFS_NONNULL(sim);
+    GFS_NONNULL(n);
+    GFS_NONNULL(h_positions);
+    GFS_NONNULL(h_velocities);
+    Sim *s = &sim->s;
+    int rc = sim_set_particles(s, h_positions, h_velocities, h_ids, *n);
+    if (rc) return rc;
+    rc = sim_step(s, dt, stats);
+    if (rc) return rc;
+    std::vector<uint32_t> tmp;
+    uint32_t *ids = h_ids;
+    if (!ids) {
+        tmp.resize((size_t)std::max<int64_t>(*n, 1));
+        ids = tmp.data();
+    }
+    return sim_get_particles(s, h_positions, h_velocities, ids, n);
+}
+
+// ---------------------------------------------------------- standalone
+
+int gfs_velocity_scalar_field(gfs_ctx *ctx, int dir, int ni, int nj, int nk, double dx,
+                              const float *h_positions, const float *h_velocities, int64_t n, float *h_field,
+                              uint8_t *h_is_set) {
+    GFS_NONNULL(ctx);
+    GFS_NONNULL(h_field);
+    GFS_NONNULL(h_is_set);
+    if (dir < 0 || dir > 2 || !valid_dims(ni, nj, nk) || !(dx > 0) || n < 0 || (n > 0 && (!h_positions || !h_velocities))) {
+        set_error(GFS_ERR_INVALID, "invalid velocity splat arguments");
+        return GFS_ERR_INVALID;
+    }
+    gfs_sim *sim = nullptr;
+    int rc = gfs_sim_create(ctx, ni, nj, nk, dx, n, &sim);
+    if (rc) return rc;
+    Sim *s = &sim->s;
+    rc = sim_set_particles(s, h_positions, h_velocities, nullptr, n);
+    if (!rc) rc = sort_particles(s, false);
+    if (!rc) rc = splat_velocity(s);
+    DevMem stage;
+    if (!rc) rc = download_padded<float>(&ctx->c, s->sval[dir].as<float>(), s->g.f[dir], h_field, stage);
+    if (!rc) rc = download_padded<uint8_t>(&ctx->c, s->smask[dir].as<uint8_t>(), s->g.f[dir], h_is_set, stage);
+    gfs_sim_destroy(sim);
+    return rc;
+}
+
+static int stage_mac(Ctx *ctx, const Grids &g, const float *hu, const float *hv, const float *hw, DevMem dm[3],
+                     DevMem &stage) {
+    const float *h[3] = {hu, hv, hw};
+    for (int d = 0; d < 3; d++) {
+        if (dm[d].alloc((size_t)g.f[d].size * sizeof(float))) return GFS_ERR_NOMEM;
+        GFS_CUDA_CHECK(cudaMemsetAsync(dm[d].p, 0, dm[d].bytes, ctx->stream));
+        int rc = upload_padded<float>(ctx, h[d], g.f[d], dm[d].as<float>(), stage);
+        if (rc) return rc;
+    }
+    return GFS_OK;
+}
+
+static int points_common(gfs_ctx *ctx, int order, int ni, int nj, int nk, double dx, const float *hu,
+                         const float *hv, const float *hw, double dt, const float *hp, int64_t n, float *hout,
+                         bool validate) {
+    GFS_NONNULL(ctx);
+    if (!valid_dims(ni, nj, nk) || !(dx > 0) || n < 0 || !hu || !hv || !hw || (n > 0 && (!hp || !hout))) {
+        set_error(GFS_ERR_INVALID, "invalid interpolation arguments");
+        return GFS_ERR_INVALID;
+    }
+    Ctx *c = &ctx->c;
+    Grids g = make_grids(ni, nj, nk, dx);
+    DevMem dm[3], stage, dp, dout;
+    int rc = stage_mac(c, g, hu, hv, hw, dm, stage);
+    if (rc) return rc;
+    if (n == 0) return GFS_OK;
+    if (dp.alloc((size_t)n * 3 * sizeof(float)) || dout.alloc((size_t)n * 3 * sizeof(float))) return GFS_ERR_NOMEM;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(dp.p, hp, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    float *mac[3] = {dm[0].as<float>(), dm[1].as<float>(), dm[2].as<float>()};
+    rc = interpolate_points(c, g, mac, dp.as<float>(), n, dout.as<float>(), order, dt, validate);
+    if (rc) return rc;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(hout, dout.p, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    GFS_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+    return GFS_OK;
+}
+
+int gfs_tricubic_interpolate(gfs_ctx *ctx, int ni, int nj, int nk, double dx, const float *h_u, const float *h_v,
+                             const float *h_w, const float *h_points, int64_t n, float *h_out) {
+    return points_common(ctx, 0, ni, nj, nk, dx, h_u, h_v, h_w, 0.0, h_points, n, h_out, true);
+}
+
+int gfs_advect_particles(gfs_ctx *ctx, int order, int ni, int nj, int nk, double dx, const float *h_u,
+                         const float *h_v, const float *h_w, double dt, const float *h_points, int64_t n,
+                         float *h_out) {
+    if (order < 1 || order > 4) {
+        set_error(GFS_ERR_INVALID, "Runge-Kutta order must be 1..4 (got %d)", order);
+        return GFS_ERR_INVALID;
+    }
+    return points_common(ctx, order, ni, nj, nk, dx, h_u, h_v, h_w, dt, h_points, n, h_out, false);
+}
+
+int gfs_pressure_solve(gfs_ctx *ctx, int ni, int nj, int nk, double dx, double density, double dt,
+                       const uint8_t *h_material, const float *h_u, const float *h_v, const float *h_w, int precision,
+                       double tol, int max_iters, double *h_pressure, int64_t *num_fluid_cells, int *iterations,
+                       double *max_residual) {
+    GFS_NONNULL(ctx);
+    GFS_NONNULL(h_material);
+    GFS_NONNULL(num_fluid_cells);
+    if (!valid_dims(ni, nj, nk) || !(dx > 0) || !(density > 0) || !(dt >= 0) ||
+        (precision != GFS_PRECISION_PLAIN && precision != GFS_PRECISION_MIXED)) {
+        set_error(GFS_ERR_INVALID, "invalid pressure-solve arguments");
+        return GFS_ERR_INVALID;
+    }
+    size_t ncell = (size_t)ni * nj * nk;
+    int64_t F = 0;
+    for (size_t q = 0; q < ncell; q++) F += h_material[q] == GFS_FLUID;
+    if (!h_pressure) {
+        *num_fluid_cells = F;
+        return GFS_OK;
+    }
+    if (*num_fluid_cells < F) {
+        set_error(GFS_ERR_INVALID, "pressure array holds %lld entries, %lld fluid cells", (long long)*num_fluid_cells,
+                  (long long)F);
+        return GFS_ERR_INVALID;
+    }
+    if (!h_u || !h_v || !h_w) {
+        set_error(GFS_ERR_INVALID, "velocity field pointers must not be NULL");
+        return GFS_ERR_INVALID;
+    }
+    *num_fluid_cells = F;
+    if (tol <= 0) tol = 1e-6;
+    if (max_iters <= 0) max_iters = 200;
+    Ctx *c = &ctx->c;
+    Grids g = make_grids(ni, nj, nk, dx);
+    DevMem dm[3], stage, mat, dout;
+    int rc = stage_mac(c, g, h_u, h_v, h_w, dm, stage);
+    if (rc) return rc;
+    if (mat.alloc((size_t)g.c.size)) return GFS_ERR_NOMEM;
+    GFS_CUDA_CHECK(cudaMemsetAsync(mat.p, GFS_SOLID, mat.bytes, c->stream));
+    rc = upload_padded<uint8_t>(c, h_material, g.c, mat.as<uint8_t>(), stage);
+    if (rc) return rc;
+    PressureWs ws;
+    float *mac[3] = {dm[0].as<float>(), dm[1].as<float>(), dm[2].as<float>()};
+    gfs_step_stats st{};
+    rc = pressure_solve(c, ws, g, mat.as<uint8_t>(), mac, density, dt, precision, tol, max_iters, &st);
+    if (rc) return rc;
+    if (iterations) *iterations = st.cg_iterations;
+    if (max_residual) *max_residual = st.cg_max_residual;
+    if (F > 0) {
+        if (dout.alloc((size_t)F * sizeof(double))) return GFS_ERR_NOMEM;
+        rc = pressure_gather_compact(c, ws, g, mat.as<uint8_t>(), dout.as<double>(), F);
+        if (rc) return rc;
+        GFS_CUDA_CHECK(cudaMemcpyAsync(h_pressure, dout.p, (size_t)F * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        GFS_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+    }
+    return GFS_OK;
+}
+
+int gfs_scalar_field_add_point_values(gfs_ctx *ctx, const float *h_points, const float *h_values, int64_t n,
+                                      double radius, const float offset[3], double dx, int W, int H, int D,
+                                      float *h_scalarfield, float *h_weightfield) {
+    GFS_NONNULL(ctx);
+    (void)h_points; (void)h_values; (void)n; (void)radius; (void)offset; (void)dx;
+    (void)W; (void)H; (void)D; (void)h_scalarfield; (void)h_weightfield;
+    set_error(GFS_ERR_STATE, "gfs_scalar_field_add_point_values: general-radius splat not available yet");
+    return GFS_ERR_STATE;
+}
+
+}  // extern "C"

@@ -1,0 +1,136 @@
+// gfs_internal.h -- host-side structures shared by the libgfs translation units.
+#pragma once
+
+#include <cstdarg>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gfs.h"
+#include "gfs_common.cuh"
+
+namespace gfs {
+
+void set_error(int code, const char *fmt, ...);
+
+// A device allocation that frees itself.
+struct DevMem {
+    void *p = nullptr;
+    size_t bytes = 0;
+    int alloc(size_t n);          // GFS_OK or GFS_ERR_NOMEM (sets the message)
+    int ensure(size_t n);         // grow-only
+    void release();
+    ~DevMem() { release(); }
+    template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+struct Ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    int64_t launches = 0;
+    char device_name[256] = {0};
+};
+
+// Controls of the pressure solve, kept in device memory so that the CG loop
+// needs no host round trip per iteration.
+struct PsCtrl {
+    double sigma, alpha, beta;   // CG scalars
+    double maxb;                 // max|b|
+    double maxr;                 // max|r| of the iteration (FP64 for PLAIN, FP32 r promoted for MIXED inner)
+    double maxr64;               // MIXED: FP64 max|b - A p| of the last refinement
+    double inner_tol;            // MIXED: inner stopping threshold
+    double tol;
+    int iter;                    // CG iteration number (reference numbering)
+    int max_iters;
+    int done;                    // loop finished (converged or capped)
+    int converged;
+    int total_inner;             // MIXED: inner iterations so far
+    int refinements;
+    unsigned err;                // GFS_DEV_ERR_* bits
+    unsigned tickets[4];         // last-block-done tickets of fused reductions
+    unsigned sweep_ticket[3];    // dispatch tickets of the wavefront kernels (fwd, bwd, precon)
+};
+
+// Dense padded pressure workspace over the cell grid.
+struct PressureWs {
+    GridDim c{};
+    int nbj = 0, nbk = 0;        // wavefront block grid
+    DevMem flags;                // uint8
+    DevMem b, p, r, z, s, As, q, precon;            // FP64
+    DevMem r32, z32, s32, As32, q32, e32, precon32; // FP32 (mixed)
+    DevMem partials;             // double per block
+    DevMem ctrl;                 // PsCtrl
+    DevMem progress;             // unsigned per wavefront block x 3 kinds
+    size_t nblocks_red = 0;      // blocks of the reduction kernels
+    long long allocated_for = -1;
+    bool mixed_alloc = false;
+};
+
+struct Sim {
+    Ctx *ctx = nullptr;
+    Grids g{};
+    gfs_sim_params params{};
+    int64_t capacity = 0;
+    int64_t n_bound = 0;         // host-side upper bound of the particle count
+    bool need_sort = false;      // particles not yet in (cell, id) order
+    bool dx_pow2 = false;
+    float inv_dx_f = 0.f;
+    float bound_f[3] = {0, 0, 0}; // smallest floats >= dx*n (exact in-grid test)
+
+    DevMem mat;                  // uint8 padded cell grid
+    DevMem mac[3], saved[3];     // float padded face grids
+    DevMem sval[3], smask[3];    // splat value / is-set mask
+    DevMem layer;                // int8 padded cell grid
+    DevMem pos, vel, pos_alt, vel_alt;   // float4 x capacity
+    DevMem key, slot;            // uint32 x capacity
+    DevMem count, offset, scan_tmp;      // uint32 x (ncells + 1), scan block sums
+    DevMem num;                  // uint32[4]: [0] particle count, [1] overflow flag
+    DevMem pgrid;                // float pressure grid (unpadded) for get_pressure
+    PressureWs ps;
+    gfs_step_stats last{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evp0 = nullptr, evp1 = nullptr;
+};
+
+// ---- particles.cu
+int sort_particles(Sim *s, bool remove_solid);
+int classify_cells(Sim *s);
+int exclusive_scan_u32(Ctx *ctx, uint32_t *data_in, uint32_t *data_out, long long n,
+                       uint32_t *block_sums, cudaStream_t st);
+size_t scan_temp_elems(long long n);
+
+// ---- splat.cu
+int splat_velocity(Sim *s);           // P2G for U, V, W into sval/smask
+int face_fill(Sim *s, double dt);     // a3 + saved copy + body forces
+// standalone weighted splat on an arbitrary node grid (device buffers)
+int splat_points_device(Ctx *ctx, const float4 *pos, const float *vals, const uint32_t *offsets,
+                        const uint32_t *perm, int cni, int cnj, int cnk, double cdx,
+                        double radius, const float offset[3], double dx, int W, int H, int D,
+                        float *field, float *weight, float *vfield, uint8_t *vmask, bool normalise);
+
+// ---- extrapolate.cu
+int build_layers(Sim *s, int num_layers);
+int extrapolate_field(Sim *s, float *const f[3], int num_layers, bool reset);
+
+// ---- pressure.cu
+int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
+                   float *const mac[3], double density, double dt, int precision, double tol,
+                   int max_iters, gfs_step_stats *stats);
+int pressure_apply(Sim *s, double dt);
+int pressure_to_grid(Ctx *ctx, PressureWs &ws, const Grids &g, float *pgrid_unpadded);
+int pressure_gather_compact(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
+                            double *d_out, int64_t F);
+
+// ---- advect.cu
+int g2p_advect(Sim *s, double dt);
+int interpolate_points(Ctx *ctx, const Grids &g, float *const mac[3], const float *d_points,
+                       int64_t n, float *d_out, int rk_order, double dt, bool validate);
+
+}  // namespace gfs
+
+struct gfs_ctx {
+    gfs::Ctx c;
+};
+
+struct gfs_sim {
+    gfs::Sim s;
+};

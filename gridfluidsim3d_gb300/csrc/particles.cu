@@ -1,0 +1,321 @@
+// particles.cu -- particle ordering and cell classification.
+//
+// Particles are kept in (cell, id) order.  After every substep (and after an
+// upload) a counting sort rebuilds that order:
+//   k_keys      cell key per particle (invalid for out-of-grid / solid cells:
+//               FluidSimulation::_removeMarkerParticlesInSolidCells,
+//               fluidsimulation.cpp:1933-1958) and an atomic slot in its cell;
+//   scan        exclusive scan of the per-cell counts -> cell offsets;
+//   k_scatter   particles to offset[cell] + slot;
+//   k_cell_sort insertion sort of each cell's run by particle id, which makes
+//               the order independent of the atomic slot order (the splat sums
+//               in this order, so every run is bitwise reproducible);
+//   cap         cells holding more than max_particles_per_cell keep their
+//               smallest ids (FluidSimulation::_removeMarkerParticles,
+//               fluidsimulation.cpp:3221-3243, keeps a random subset after a
+//               rand() shuffle; the selection here is deterministic).
+// k_classify is FluidSimulation::_updateFluidCells (fluidsimulation.cpp:1990-2041)
+// on the dense grid: interior fluid cells become air, cells holding particles
+// become fluid.  The lexicographic fluid-cell list of the reference is implicit
+// in the dense layout.
+#include <utility>
+
+#include "gfs_internal.h"
+
+namespace gfs {
+
+#define KEY_INVALID 0xFFFFFFFFu
+
+__device__ __forceinline__ uint32_t pid(const float4 &p) { return __float_as_uint(p.w); }
+
+__global__ void k_keys(const float4 *__restrict__ pos, const uint32_t *__restrict__ num,
+                       long long nbound, GridDim c, double invdx_d, float invdx_f, int pow2,
+                       const uint8_t *__restrict__ mat, uint32_t *__restrict__ key,
+                       uint32_t *__restrict__ slot, uint32_t *__restrict__ count) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= nbound || p >= (long long)num[0]) return;
+    float4 x = pos[p];
+    uint32_t kk = KEY_INVALID;
+    if (isfinite(x.x) && isfinite(x.y) && isfinite(x.z)) {
+        int i, j, k;
+        // Grid3d::positionToGridIndex (grid3d.h:58-63): floor(p * (1/dx)).  With
+        // a power-of-two dx the float product is exact and equals the double one.
+        if (pow2) {
+            i = (int)floorf(x.x * invdx_f);
+            j = (int)floorf(x.y * invdx_f);
+            k = (int)floorf(x.z * invdx_f);
+        } else {
+            i = (int)floor((double)x.x * invdx_d);
+            j = (int)floor((double)x.y * invdx_d);
+            k = (int)floor((double)x.z * invdx_d);
+        }
+        if (c.in(i, j, k) && mat[c.at(i, j, k)] != GFS_SOLID)
+            kk = (uint32_t)i + (uint32_t)c.nx * ((uint32_t)j + (uint32_t)c.ny * (uint32_t)k);
+    }
+    key[p] = kk;
+    if (kk != KEY_INVALID) slot[p] = atomicAdd(&count[kk], 1u);
+}
+
+__global__ void k_scatter(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                          const uint32_t *__restrict__ key, const uint32_t *__restrict__ slot,
+                          const uint32_t *__restrict__ offset, const uint32_t *__restrict__ num,
+                          long long nbound, float4 *__restrict__ pos_out,
+                          float4 *__restrict__ vel_out) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= nbound || p >= (long long)num[0]) return;
+    uint32_t kk = key[p];
+    if (kk == KEY_INVALID) return;
+    uint32_t d = offset[kk] + slot[p];
+    pos_out[d] = pos[p];
+    vel_out[d] = vel[p];
+}
+
+// One thread per cell: insertion sort of the cell's run by id, in place.
+__global__ void k_cell_sort(float4 *__restrict__ pos, float4 *__restrict__ vel,
+                            const uint32_t *__restrict__ offset, long long ncells, int cap,
+                            uint32_t *__restrict__ num) {
+    long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    uint32_t b = offset[c], e = offset[c + 1];
+    if (c == ncells - 1) num[0] = e;    // particle count after removal
+    uint32_t m = e - b;
+    if ((int)m > cap) atomicOr(&num[1], 1u);
+    if (m <= 1) return;
+    for (uint32_t a = b + 1; a < e; a++) {
+        float4 cp = pos[a];
+        uint32_t cid = pid(cp);
+        if (pid(pos[a - 1]) <= cid) continue;
+        float4 cv = vel[a];
+        uint32_t t = a;
+        while (t > b && pid(pos[t - 1]) > cid) {
+            pos[t] = pos[t - 1];
+            vel[t] = vel[t - 1];
+            t--;
+        }
+        pos[t] = cp;
+        vel[t] = cv;
+    }
+}
+
+__global__ void k_cap_counts(const uint32_t *__restrict__ offset, long long ncells, int cap,
+                             uint32_t *__restrict__ cnt) {
+    long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (c > ncells) return;
+    if (c == ncells) { cnt[c] = 0; return; }
+    uint32_t m = offset[c + 1] - offset[c];
+    cnt[c] = m < (uint32_t)cap ? m : (uint32_t)cap;
+}
+
+__global__ void k_cap_copy(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                           const uint32_t *__restrict__ off_in, const uint32_t *__restrict__ off_out,
+                           long long ncells, float4 *__restrict__ pos_out,
+                           float4 *__restrict__ vel_out, uint32_t *__restrict__ num) {
+    long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    uint32_t b = off_in[c], o = off_out[c], m = off_out[c + 1] - o;
+    for (uint32_t a = 0; a < m; a++) {
+        pos_out[o + a] = pos[b + a];
+        vel_out[o + a] = vel[b + a];
+    }
+    if (c == ncells - 1) num[0] = off_out[ncells];
+}
+
+// ------------------------------------------------------------------ scan
+
+#define SCAN_THREADS 512
+#define SCAN_ITEMS 16
+#define SCAN_TILE (SCAN_THREADS * SCAN_ITEMS)
+
+size_t scan_temp_elems(long long n) { return (size_t)((n + SCAN_TILE - 1) / SCAN_TILE) + 1; }
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *total) {
+    __shared__ uint32_t warp_sums[SCAN_THREADS / 32];
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < SCAN_THREADS / 32 ? warp_sums[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < SCAN_THREADS / 32) warp_sums[lane] = w;
+    }
+    __syncthreads();
+    uint32_t before = warp > 0 ? warp_sums[warp - 1] : 0;
+    *total = warp_sums[SCAN_THREADS / 32 - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+// in and out may alias (the cap path scans in place).
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_local(const uint32_t *in, uint32_t *out, long long n,
+                                                             uint32_t *__restrict__ block_sums) {
+    long long base = (long long)blockIdx.x * SCAN_TILE + (long long)threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int q = 0; q < SCAN_ITEMS; q++) {
+        long long e = base + q;
+        v[q] = e < n ? in[e] : 0u;
+        sum += v[q];
+    }
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(sum, &total);
+#pragma unroll
+    for (int q = 0; q < SCAN_ITEMS; q++) {
+        long long e = base + q;
+        if (e < n) out[e] = run;
+        run += v[q];
+    }
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_top(uint32_t *__restrict__ sums, long long nb) {
+    // nb <= SCAN_TILE
+    long long base = (long long)threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int q = 0; q < SCAN_ITEMS; q++) {
+        long long e = base + q;
+        v[q] = e < nb ? sums[e] : 0u;
+        sum += v[q];
+    }
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(sum, &total);
+#pragma unroll
+    for (int q = 0; q < SCAN_ITEMS; q++) {
+        long long e = base + q;
+        if (e < nb) sums[e] = run;
+        run += v[q];
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_add(uint32_t *__restrict__ out, long long n,
+                                                           const uint32_t *__restrict__ sums) {
+    uint32_t add = sums[blockIdx.x];
+    long long base = (long long)blockIdx.x * SCAN_TILE;
+    for (int q = threadIdx.x; q < SCAN_TILE; q += SCAN_THREADS) {
+        long long e = base + q;
+        if (e < n) out[e] += add;
+    }
+}
+
+int exclusive_scan_u32(Ctx *ctx, uint32_t *in, uint32_t *out, long long n, uint32_t *block_sums,
+                       cudaStream_t st) {
+    long long nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (nb > SCAN_TILE) {
+        set_error(GFS_ERR_INVALID, "scan of %lld elements exceeds the supported %lld", n,
+                  (long long)SCAN_TILE * SCAN_TILE);
+        return GFS_ERR_INVALID;
+    }
+    k_scan_local<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, out, n, block_sums);
+    k_scan_top<<<1, SCAN_THREADS, 0, st>>>(block_sums, nb);
+    k_scan_add<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(out, n, block_sums);
+    ctx->launches += 3;
+    GFS_LAUNCH_CHECK();
+    return GFS_OK;
+}
+
+// --------------------------------------------------------------- driver
+
+int sort_particles(Sim *s, bool /*remove_solid*/) {
+    Ctx *ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    const GridDim &c = s->g.c;
+    long long ncells = (long long)c.nx * c.ny * c.nz;
+    long long nb = s->n_bound;
+    uint32_t *count = s->count.as<uint32_t>();
+    uint32_t *offset = s->offset.as<uint32_t>();
+    uint32_t *num = s->num.as<uint32_t>();
+    GFS_CUDA_CHECK(cudaMemsetAsync(count, 0, (size_t)(ncells + 1) * sizeof(uint32_t), st));
+    GFS_CUDA_CHECK(cudaMemsetAsync(num + 1, 0, sizeof(uint32_t), st));
+    const int T = 256;
+    if (nb > 0) {
+        k_keys<<<grid_blocks(nb, T), T, 0, st>>>(s->pos.as<float4>(), num, nb, c, 1.0 / s->g.dx,
+                                                 s->inv_dx_f, s->dx_pow2 ? 1 : 0, s->mat.as<uint8_t>(),
+                                                 s->key.as<uint32_t>(), s->slot.as<uint32_t>(), count);
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+    }
+    int rc = exclusive_scan_u32(ctx, count, offset, ncells + 1, s->scan_tmp.as<uint32_t>(), st);
+    if (rc) return rc;
+    if (nb > 0) {
+        k_scatter<<<grid_blocks(nb, T), T, 0, st>>>(s->pos.as<float4>(), s->vel.as<float4>(),
+                                                    s->key.as<uint32_t>(), s->slot.as<uint32_t>(),
+                                                    offset, num, nb, s->pos_alt.as<float4>(),
+                                                    s->vel_alt.as<float4>());
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+    }
+    std::swap(s->pos.p, s->pos_alt.p);
+    std::swap(s->vel.p, s->vel_alt.p);
+    int cap = s->params.max_particles_per_cell > 0 ? s->params.max_particles_per_cell : 0x7fffffff;
+    k_cell_sort<<<grid_blocks(ncells, T), T, 0, st>>>(s->pos.as<float4>(), s->vel.as<float4>(),
+                                                      offset, ncells, cap, num);
+    ctx->launches++;
+    GFS_LAUNCH_CHECK();
+    uint32_t host_num[2];
+    GFS_CUDA_CHECK(cudaMemcpyAsync(host_num, num, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GFS_CUDA_CHECK(cudaStreamSynchronize(st));
+    if (host_num[1]) {
+        // Some cell holds more than `cap` particles: keep the smallest ids.
+        k_cap_counts<<<grid_blocks(ncells + 1, T), T, 0, st>>>(offset, ncells, cap, count);
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+        rc = exclusive_scan_u32(ctx, count, count, ncells + 1, s->scan_tmp.as<uint32_t>(), st);
+        if (rc) return rc;
+        k_cap_copy<<<grid_blocks(ncells, T), T, 0, st>>>(s->pos.as<float4>(), s->vel.as<float4>(),
+                                                         offset, count, ncells, s->pos_alt.as<float4>(),
+                                                         s->vel_alt.as<float4>(), num);
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+        std::swap(s->pos.p, s->pos_alt.p);
+        std::swap(s->vel.p, s->vel_alt.p);
+        std::swap(s->count.p, s->offset.p);   // capped offsets become the live offsets
+        GFS_CUDA_CHECK(cudaMemcpyAsync(host_num, num, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        GFS_CUDA_CHECK(cudaStreamSynchronize(st));
+    }
+    s->n_bound = host_num[0];
+    s->need_sort = false;
+    return GFS_OK;
+}
+
+__global__ void k_classify(uint8_t *__restrict__ mat, GridDim c, const uint32_t *__restrict__ offset,
+                           uint32_t *__restrict__ fluid_count) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y, k = blockIdx.z;
+    bool fl = false;
+    if (i < c.nx) {
+        long long at = c.at(i, j, k);
+        uint8_t m = mat[at];
+        bool interior = i > 0 && j > 0 && k > 0 && i < c.nx - 1 && j < c.ny - 1 && k < c.nz - 1;
+        if (interior && m == GFS_FLUID) m = GFS_AIR;
+        long long lin = i + (long long)c.nx * (j + (long long)c.ny * k);
+        if (offset[lin + 1] > offset[lin]) m = GFS_FLUID;
+        mat[at] = m;
+        fl = m == GFS_FLUID;
+    }
+    unsigned b = __ballot_sync(0xffffffffu, fl);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(fluid_count, (uint32_t)__popc(b));
+}
+
+int classify_cells(Sim *s) {
+    Ctx *ctx = s->ctx;
+    const GridDim &c = s->g.c;
+    uint32_t *num = s->num.as<uint32_t>();
+    GFS_CUDA_CHECK(cudaMemsetAsync(num + 2, 0, sizeof(uint32_t), ctx->stream));
+    dim3 grid(grid_blocks(c.nx, 128), c.ny, c.nz);
+    k_classify<<<grid, 128, 0, ctx->stream>>>(s->mat.as<uint8_t>(), c, s->offset.as<uint32_t>(), num + 2);
+    ctx->launches++;
+    GFS_LAUNCH_CHECK();
+    return GFS_OK;
+}
+
+}  // namespace gfs

@@ -1,0 +1,217 @@
+/*
+ * gfs.h -- C ABI of libgfs, the GB300 (sm_103a) per-substep FLIP core of
+ * GridFluidSim3D: marker-particle -> MAC-grid velocity splat, MICCG(0)
+ * pressure projection, PIC/FLIP grid -> particle update with RK4 advection.
+ *
+ * Conventions (all entry points):
+ *   - every call returns int status: GFS_OK (0) or a GFS_ERR_* code; the message
+ *     of the last failure on the calling thread is gfs_last_error().  This is
+ *     the reference's c_bindings convention (cbindings.h:20-135: a status plus a
+ *     global error string) without exceptions crossing the ABI;
+ *   - grids are flat float/uint8 arrays in the reference's Array3d order,
+ *     index i + W*(j + H*k) (array3d.h:394-402); U is (ni+1) x nj x nk,
+ *     V is ni x (nj+1) x nk, W is ni x nj x (nk+1); material is uint8,
+ *     0 air, 1 fluid, 2 solid (fluidmaterialgrid.h:29-33);
+ *   - particle positions / velocities are float xyz triples (vmath::vec3,
+ *     vmath.h:33-56); ids are uint32 and travel with their particle;
+ *   - pointers named h_* are host memory, borrowed for the duration of the call
+ *     (pinned memory makes the copies asynchronous-capable and faster);
+ *   - a gfs_ctx owns one CUDA stream and its device buffers; calls on one
+ *     context must come from one thread at a time (the reference is
+ *     single-threaded).
+ */
+#ifndef GFS_H
+#define GFS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GFS_OK 0
+#define GFS_ERR_INVALID 1   /* bad argument (sizes, null pointers, dt < 0 ...) */
+#define GFS_ERR_CUDA 2      /* CUDA runtime error (message names the call)     */
+#define GFS_ERR_NOMEM 3     /* device allocation failed                        */
+#define GFS_ERR_TIMEOUT 4   /* a wavefront wait hit its bound (device status)  */
+#define GFS_ERR_STATE 5     /* call out of order (e.g. step before particles)  */
+
+/* Pressure-solve precision. PLAIN: FP64 vectors, stencil, preconditioner and
+   dots, the reference's arithmetic (pressuresolver.cpp).  MIXED: FP32 vectors,
+   stencil and MIC(0) apply, FP64 dots/norms and an FP64 iterative-refinement
+   residual r = b - A p; the stopping rule (max|r| < tol, evaluated in FP64) is
+   the reference's. */
+#define GFS_PRECISION_PLAIN 0
+#define GFS_PRECISION_MIXED 1
+
+typedef struct gfs_ctx gfs_ctx;
+typedef struct gfs_sim gfs_sim;
+
+/* ------------------------------------------------------------- library */
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *gfs_last_error(void);
+/* Library version string. */
+const char *gfs_version(void);
+
+/* ------------------------------------------------------------- context */
+
+/* Create a context on CUDA device `device` (its own non-blocking stream).
+   Replaces the OpenCL context set-up of CLScalarField::initialize
+   (clscalarfield.cpp:33-66) and ParticleAdvector::initialize
+   (particleadvector.cpp:33-63). */
+int gfs_ctx_create(int device, gfs_ctx **out);
+int gfs_ctx_destroy(gfs_ctx *ctx);
+/* Wait for all work queued on the context's stream. */
+int gfs_ctx_synchronize(gfs_ctx *ctx);
+/* The context's cudaStream_t, for callers that time or order work on it. */
+int gfs_ctx_stream(gfs_ctx *ctx, void **stream);
+/* Device name (cf. getDeviceInfo, clscalarfield.h:112 / particleadvector.h:72). */
+int gfs_ctx_device_name(gfs_ctx *ctx, char *buf, int buflen);
+
+/* ------------------------------------------- splat (CLScalarField drop-in) */
+
+/* Weighted point splat: for every point p with value v, every grid node x within
+   `radius` of p - offset receives  field += w*v  and  weight += w  with
+   w = 1 - 4/9 s^3 + 17/9 s^2 - 22/9 s, s = |x - p|^2 / radius^2.
+   Replaces CLScalarField::addPointValues(points, values, radius, offset, dx,
+   scalarfield, weightfield) (clscalarfield.h:84-90, clscalarfield.cpp:200-267)
+   and its kernel compute_scalar_field_weight_point_values
+   (kernels/scalarfield.cl:202-268).  Adds into the caller's arrays ("add"
+   semantics of the reference's accelerated path, clscalarfield.cpp:1413,1448).
+   h_weightfield may be NULL: then only field += w*v is formed
+   (addPointValues without weight field, clscalarfield.h:78-83).
+   Field dims W x H x D; node (i,j,k) sits at (i,j,k)*dx. */
+int gfs_scalar_field_add_point_values(gfs_ctx *ctx, const float *h_points, const float *h_values,
+                                      int64_t n, double radius, const float offset[3], double dx,
+                                      int W, int H, int D, float *h_scalarfield,
+                                      float *h_weightfield);
+
+/* Velocity splat of one MAC component: FluidSimulation::_computeVelocityScalarField
+   (fluidsimulation.cpp:2526-2595): weighted splat of velocity[dir] with radius dx
+   and the face offset of `dir`, then field /= weight where weight > 0
+   (ScalarField::applyWeightField, scalarfield.cpp:90-106) and
+   is_set = weight > 1e-9.  Outputs are the face grid of `dir` (fully written). */
+int gfs_velocity_scalar_field(gfs_ctx *ctx, int dir, int ni, int nj, int nk, double dx,
+                              const float *h_positions, const float *h_velocities, int64_t n,
+                              float *h_field, uint8_t *h_is_set);
+
+/* ------------------------------------- G2P / RK (ParticleAdvector drop-in) */
+
+/* Catmull-Rom tricubic velocity at each point from a MAC field.
+   Replaces ParticleAdvector::tricubicInterpolate(particles, vfield, output)
+   (particleadvector.h:101-103, particleadvector.cpp:401-455) and its kernel
+   tricubic_interpolate_kernel (kernels/tricubicinterpolate.cl:279-328);
+   the arithmetic follows MACVelocityField::evaluateVelocityAtPosition
+   (macvelocityfield.cpp:549-559).  Non-finite results become 0
+   (ParticleAdvector::_validateOutput, particleadvector.cpp:1139-1149). */
+int gfs_tricubic_interpolate(gfs_ctx *ctx, int ni, int nj, int nk, double dx, const float *h_u,
+                             const float *h_v, const float *h_w, const float *h_points,
+                             int64_t n, float *h_out);
+
+/* Runge-Kutta advection of order 1..4 through a MAC field.
+   Replaces ParticleAdvector::advectParticlesRK4/3/2/1
+   (particleadvector.h:80-98, particleadvector.cpp:209-399; formulas of
+   _RK4/_RK3/_RK2/_RK1 :1045-1078). */
+int gfs_advect_particles(gfs_ctx *ctx, int order, int ni, int nj, int nk, double dx,
+                         const float *h_u, const float *h_v, const float *h_w, double dt,
+                         const float *h_points, int64_t n, float *h_out);
+
+/* -------------------------------------- pressure (PressureSolver drop-in) */
+
+/* MICCG(0) pressure solve.  Replaces PressureSolver::solve(params, pressure)
+   (pressuresolver.h:117, pressuresolver.cpp:116-498).  Fluid cells are the
+   material's fluid cells in lexicographic k->j->i order, the order
+   FluidSimulation::_updateFluidCells builds (fluidsimulation.cpp:2031-2039);
+   h_pressure receives one double per fluid cell in that order and must hold
+   *num_fluid_cells entries (call with h_pressure = NULL to query the count).
+   tol <= 0 / max_iters <= 0 select the reference's 1e-6 / 200
+   (pressuresolver.h:159-160).  *iterations is the CG iteration number the
+   reference logs (pressuresolver.cpp:477, 200 when the cap is hit, -1 when
+   max|b| < tol); for MIXED it counts inner FP32 iterations. */
+int gfs_pressure_solve(gfs_ctx *ctx, int ni, int nj, int nk, double dx, double density,
+                       double dt, const uint8_t *h_material, const float *h_u,
+                       const float *h_v, const float *h_w, int precision, double tol,
+                       int max_iters, double *h_pressure, int64_t *num_fluid_cells,
+                       int *iterations, double *max_residual);
+
+/* ------------------------------ device-resident substep (FluidSimulation) */
+
+typedef struct gfs_sim_params {
+    double density;          /* _density = 20 (fluidsimulation.h:1154)                  */
+    double ratio_pic;        /* _ratioPICFLIP = 0.05f (fluidsimulation.h:1161)          */
+    double cfl;              /* _CFLConditionNumber = 5 -> ceil(cfl+2) extrapolation layers */
+    float gravity[3];        /* sum of constant body forces (fluidsimulation.cpp:2758)  */
+    int max_particles_per_cell; /* _maxMarkerParticlesPerCell = 100 (fluidsimulation.h:1167) */
+    int precision;           /* GFS_PRECISION_PLAIN / GFS_PRECISION_MIXED               */
+    double tol;              /* pressure tolerance, max|r| (pressuresolver.h:159)       */
+    int max_cg_iterations;   /* 200 (pressuresolver.h:160)                              */
+} gfs_sim_params;
+
+typedef struct gfs_step_stats {
+    int64_t num_particles;
+    int64_t num_fluid_cells;
+    int cg_iterations;       /* as gfs_pressure_solve                                   */
+    int refinements;         /* MIXED: outer FP64 refinement steps                      */
+    double cg_max_residual;  /* FP64 max|b - A p| at exit                               */
+    double pressure_ms;      /* device time of the pressure solve                       */
+    double step_ms;          /* device time of the whole substep                        */
+} gfs_step_stats;
+
+/* Fill p with the reference's defaults. */
+int gfs_sim_default_params(gfs_sim_params *p);
+
+/* A simulation of ni x nj x nk cells of width dx holding up to max_particles
+   particles on the device (the state FluidSimulation keeps in _markerParticles,
+   _materialGrid and _MACVelocity, fluidsimulation.h:1047-1171). */
+int gfs_sim_create(gfs_ctx *ctx, int ni, int nj, int nk, double dx, int64_t max_particles,
+                   gfs_sim **out);
+int gfs_sim_destroy(gfs_sim *sim);
+int gfs_sim_set_params(gfs_sim *sim, const gfs_sim_params *p);
+int gfs_sim_get_params(gfs_sim *sim, gfs_sim_params *p);
+/* Material grid in (ni*nj*nk uint8).  Particles in solid cells are removed
+   at the next step, as FluidSimulation::_removeMarkerParticlesInSolidCells does
+   (fluidsimulation.cpp:1933-1958). */
+int gfs_sim_set_material(gfs_sim *sim, const uint8_t *h_material);
+int gfs_sim_get_material(gfs_sim *sim, uint8_t *h_material);
+/* Replace the particle set (host -> device). ids may be NULL (0..n-1). */
+int gfs_sim_set_particles(gfs_sim *sim, const float *h_positions, const float *h_velocities,
+                          const uint32_t *h_ids, int64_t n);
+/* Current particle count (may sync the stream). */
+int gfs_sim_num_particles(gfs_sim *sim, int64_t *n);
+/* Particles device -> host, in the device's (cell, id) order.  Arrays must hold
+   gfs_sim_num_particles entries; any pointer may be NULL. */
+int gfs_sim_get_particles(gfs_sim *sim, float *h_positions, float *h_velocities,
+                          uint32_t *h_ids, int64_t *n);
+/* The MAC velocity field after the last step (post-extrapolation). */
+int gfs_sim_get_velocity_field(gfs_sim *sim, float *h_u, float *h_v, float *h_w);
+/* The float pressure grid of the last step (0 outside fluid). */
+int gfs_sim_get_pressure_grid(gfs_sim *sim, float *h_pressure);
+
+/* One FLIP substep of length dt on the device-resident state: stages 1, 5-9,
+   11, 12 of FluidSimulation::_stepFluid (fluidsimulation.cpp:3262-3390), i.e.
+   _updateFluidCells, _advectVelocityField (+ saved field, extrapolation),
+   _applyBodyForcesToVelocityField, _updatePressureGrid,
+   _applyPressureToVelocityField, _extrapolateFluidVelocities,
+   _updateMarkerParticleVelocities and _advanceMarkerParticles.  Meshing, level
+   set, diffuse material and fluid sources are not part of it.  stats may be
+   NULL; filling it synchronises the stream. */
+int gfs_sim_step(gfs_sim *sim, double dt, gfs_step_stats *stats);
+
+/* The same substep called the way the reference's host code would call it:
+   particles arrive in host arrays, are copied to the device, stepped, and copied
+   back (h_ids may be NULL).  On return *n holds the surviving count and the
+   arrays hold the new state in (cell, id) order.  Arrays must have room for the
+   input count. */
+int gfs_sim_step_host(gfs_sim *sim, double dt, float *h_positions, float *h_velocities,
+                      uint32_t *h_ids, int64_t *n, gfs_step_stats *stats);
+
+/* Number of kernel launches the library has issued on this context (for
+   accounting in benchmarks). */
+int gfs_ctx_launch_count(gfs_ctx *ctx, int64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GFS_H */
