@@ -1,0 +1,440 @@
+#!/usr/bin/env python3
+"""FLIP substeps/s on GB300 for the 256^3 throughput scene.
+
+Workload: 256^3 MAC grid, dx = 1/32, solid border, fluid slab y < 0.3 L plus 20
+spheres of radius U(4, 12) cells centred in y in [0.3 L, 0.9 L] (seed 3),
+8 particles per fluid cell uniform in the cell, velocities N(0, 0.5^2) per
+component, gravity (0, -25, 0), FLIP 0.95, dt = 1/30 (one substep per frame,
+as the reference runs).  A step is one FLIP substep: classification, velocity
+splat, face fill, extrapolation, body force, MICCG(0) pressure solve to the
+reference's rule (max|r| < 1e-6, cap 200), pressure update, extrapolation,
+PIC/FLIP update, RK4 advection with collisions, particle re-sort.
+
+value      substeps/s of the MIXED-precision form, state resident in HBM
+           (inputs of 40M particles x 32 B >> L2, so no flush is needed).
+plain      the same K substeps with the FP64 (PLAIN) form, from the same state.
+e2e        substeps/s through gfs_sim_step_host: particles copied from pinned
+           host memory to the device and back inside every step.
+roofline   the dominant kernel class of the timed region: algorithmic bytes per
+           launch / average device time per working launch (CUDA events on the
+           library's stream), against MEASURED_PEAKS.json's HBM copy bandwidth.
+cpu_baseline  the oracle (C restatement of the reference's CPU path, single
+           thread like the reference) timed on a bounded sample of this workload
+           and scaled to one substep.
+
+--impl reference times that CPU path alone and prints its own line.
+--gpus N (under torchrun): N independent replicas (the exact MIC(0)
+preconditioner does not partition), value = total substeps / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FLIP substeps/s at 256^3 (mixed vs plain, 1e-6 resid); fwd+adjoint ms/step"
+UNIT = "substeps/s"
+SCENE = dict(n=256, dx=1.0 / 32.0, seed=3)
+
+# Algorithmic bytes per unit of each kernel class (units: fluid cells for the
+# pressure kernels, particles for g2p / sort, face nodes for the splat).
+# FP32 (MIXED) sweeps: forward reads r, precon (4+4) and flags (1), writes q (4);
+# backward reads q, precon, r (12) and flags (1), writes z (4).  FP64 doubles the
+# vector bytes.  Matvec reads s (4|8) + flags (1), writes As; axpy reads p, r, s,
+# As and flags, writes p, r.
+BYTES = {
+    ("mic0_forward", 1): 13, ("mic0_backward", 1): 17, ("matvec", 1): 9, ("axpy", 1): 25,
+    ("update_search", 1): 13,
+    ("mic0_forward", 0): 25, ("mic0_backward", 0): 33, ("matvec", 0): 17, ("axpy", 0): 49,
+    ("update_search", 0): 25,
+    ("g2p_advect", 0): 64, ("g2p_advect", 1): 64,   # read pos4+vel4, write pos4+vel4
+}
+
+
+def rank_info():
+    r = int(os.environ.get("RANK", "0"))
+    w = int(os.environ.get("WORLD_SIZE", "1"))
+    lr = int(os.environ.get("LOCAL_RANK", "0"))
+    return r, w, lr
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 8:
+                    continue
+                try:
+                    sm.append(float(parts[0]))
+                    mx.append(float(parts[1]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[4:8]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_scene():
+    from gridfluidsim3d_gb300 import scenes
+    return scenes.slab_spheres(**SCENE)
+
+
+# --------------------------------------------------------------- CPU leg
+
+def cpu_estimate(sc, iters, sample_particles=400_000, seed=0):
+    """Single-thread oracle time of one substep of this workload, from a bounded
+    sample: every grid-wide stage at full size, the per-particle stages on a
+    random particle sample scaled to the full count, and the pressure solve's
+    set-up plus per-iteration cost scaled to `iters` CG iterations."""
+    import oracle as O
+    dims, dx, dt = sc.dims, sc.dx, sc.dt
+    g = np.array(sc.gravity, np.float32)
+    t_all = time.perf_counter()
+    mat = sc.mat.copy()
+    pos, vel, ids = sc.pos.copy(), sc.vel.copy(), sc.ids.copy()
+    t0 = time.perf_counter()
+    n = O.lib().gfo_update_fluid_cells(*dims, dx, mat, pos, vel, ids, len(pos))
+    t_classify = time.perf_counter() - t0
+    pos, vel = pos[:n], vel[:n]
+    rng = np.random.default_rng(seed)
+    sel = rng.choice(n, size=min(sample_particles, n), replace=False)
+    sp, sv = pos[sel], vel[sel]
+    scale = n / len(sel)
+    # splat: grid-only part (0 particles) + per-particle part
+    t0 = time.perf_counter()
+    u, v, w = O.advect_velocity_field(dims, dx, mat, sp[:0], sv[:0])
+    t_grid_splat = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    u, v, w = O.advect_velocity_field(dims, dx, mat, sp, sv)
+    t_part_splat = max(time.perf_counter() - t0 - t_grid_splat, 0.0) * scale
+    t0 = time.perf_counter()
+    su, sv_, sw = O.extrapolate(dims, mat, 7, u, v, w)
+    t_extrap = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    u, v, w = O.body_force(dims, mat, g, dt, u, v, w)
+    t_body = time.perf_counter() - t0
+    # pressure: set-up + per-iteration slope from two capped solves
+    m1, m2 = 2, 6
+    t0 = time.perf_counter()
+    O.pressure_solve(dims, dx, 20.0, dt, mat, u, v, w, max_iters=m1)
+    ta = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    p, _, _ = O.pressure_solve(dims, dx, 20.0, dt, mat, u, v, w, max_iters=m2)
+    tb = time.perf_counter() - t0
+    per_it = max((tb - ta) / (m2 - m1), 0.0)
+    t_setup = max(ta - m1 * per_it, 0.0)
+    t_pressure = t_setup + per_it * max(iters, 0)
+    pg = O.pressure_to_grid(dims, mat, p)
+    t0 = time.perf_counter()
+    u, v, w = O.apply_pressure(dims, dx, 20.0, dt, mat, pg, u, v, w)
+    t_apply = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    u, v, w = O.extrapolate(dims, mat, 7, u, v, w)
+    t_extrap += time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.flip_update(dims, dx, float(np.float32(0.05)), (u, v, w), (su, sv_, sw), sp, sv)
+    p1 = O.advect_rk4(dims, dx, u, v, w, dt, sp)
+    O.resolve_collisions(dims, dx, mat, sp, p1)
+    t_g2p = (time.perf_counter() - t0) * scale
+    total = (t_classify + t_grid_splat + t_part_splat + t_extrap + t_body + t_pressure + t_apply + t_g2p)
+    parts = dict(classify=t_classify, splat_grid=t_grid_splat, splat_particles=t_part_splat, extrapolate=t_extrap,
+                 body_force=t_body, pressure=t_pressure, pressure_setup=t_setup, pressure_per_iter=per_it,
+                 apply_pressure=t_apply, g2p_rk4=t_g2p)
+    return total, parts, time.perf_counter() - t_all, len(sel), n
+
+
+def reference_main(args):
+    r, world, _ = rank_info()
+    if r != 0:
+        return 0
+    sc = make_scene()
+    iters = args.ref_cg_iterations
+    times = []
+    wall = 0.0
+    for s in range(args.warmup + args.steps):
+        tot, parts, w, ns, n = cpu_estimate(sc, iters, seed=s)
+        wall += w
+        if s >= args.warmup:
+            times.append(tot)
+    t = statistics.mean(times)
+    value = 1.0 / t
+    sample = (f"per step: oracle single-thread, all grid-wide stages of the 256^3 scene at full size, "
+              f"particle stages on {ns} of {n} particles scaled x{n / ns:.1f}, pressure set-up + "
+              f"per-iteration cost scaled to {iters} CG iterations (PLAIN FP64, the reference's solver)")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 particles/grid, f64 PCG", "data": "synthetic (seeded)",
+            "impl": "reference",
+            "config": {"workload": "slab_spheres 256^3 dx=1/32, ~40M particles, 1 substep of 1/30 s",
+                       "particles": n, "parallelism": "none (single-threaded CPU)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample,
+                             "stage_seconds": {k: round(v, 4) for k, v in parts.items()}},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------- GPU leg
+
+def run_steps(sim, sc, k, dt):
+    stats = []
+    for _ in range(k):
+        stats.append(sim.update(dt))
+    return stats
+
+
+def reset(sim, sc):
+    sim.set_material_grid(sc.mat)
+    sim.set_marker_particles(sc.pos, sc.vel, sc.ids)
+
+
+def timed(ctx, sim, sc, k, dt, barrier):
+    import torch
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    l0 = ctx.launch_count()
+    e0.record(stream)
+    stats = run_steps(sim, sc, k, dt)
+    e1.record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    return e0.elapsed_time(e1) / 1e3, stats, ctx.launch_count() - l0
+
+
+def profile_read(ctx):
+    import ctypes
+    from gridfluidsim3d_gb300 import _lib
+    L = _lib.lib()
+    out = {}
+    for i in range(16):
+        nm = ctypes.c_char_p()
+        ms = ctypes.c_double()
+        cnt = ctypes.c_int64()
+        L.gfs_ctx_profile_read(ctx.handle, i, ctypes.byref(nm), ctypes.byref(ms), ctypes.byref(cnt))
+        out[nm.value.decode()] = (ms.value, cnt.value)
+    return out
+
+
+def main(args):
+    if args.impl == "reference":
+        return reference_main(args)
+    import torch
+    import torch.distributed as dist
+    from gridfluidsim3d_gb300 import PRECISION_MIXED, PRECISION_PLAIN, Context, FluidSimulation, _lib
+    from gridfluidsim3d_gb300 import build as gb
+
+    r, world, lr = rank_info()
+    torch.cuda.set_device(lr)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    gb.build()
+    _lib.load()
+    sc = make_scene()
+    ctx = Context(lr)
+    sim = FluidSimulation(*sc.dims, sc.dx, max_particles=sc.num_particles, ctx=ctx)
+    dt = sc.dt
+    peak, peak_kind = load_peaks()
+
+    results = {}
+    for name, prec in (("plain", PRECISION_PLAIN), ("mixed", PRECISION_MIXED)):
+        sim.precision = prec
+        reset(sim, sc)
+        run_steps(sim, sc, args.warmup, dt)
+        _lib.lib().gfs_ctx_profile_reset(ctx.handle)
+        _lib.lib().gfs_ctx_profile_enable(ctx.handle, 1)
+        with Clocks(lr) as clk:
+            t, stats, launches = timed(ctx, sim, sc, args.steps, dt, barrier)
+        _lib.lib().gfs_ctx_profile_enable(ctx.handle, 0)
+        prof = profile_read(ctx)
+        tmax = torch.tensor([t], dtype=torch.float64, device="cuda")
+        if world > 1:
+            dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        results[name] = dict(t=float(tmax.item()), stats=stats, launches=launches, prof=prof, clocks=clk.summary())
+
+    # end-to-end through the host-buffer entry point (mixed form)
+    sim.precision = PRECISION_MIXED
+    n0 = sc.num_particles
+    hp = torch.empty((n0, 3), dtype=torch.float32, pin_memory=True)
+    hv = torch.empty((n0, 3), dtype=torch.float32, pin_memory=True)
+    hi = torch.empty((n0,), dtype=torch.int32, pin_memory=True)
+    hp.numpy()[:] = sc.pos
+    hv.numpy()[:] = sc.vel
+    hi.numpy().view(np.uint32)[:] = sc.ids
+    sim.set_material_grid(sc.mat)
+    pos_np, vel_np, ids_np = hp.numpy(), hv.numpy(), hi.numpy().view(np.uint32)
+    n = n0
+    h2d = d2h = 0
+    for _ in range(args.warmup):
+        n, _ = sim.update_host(dt, pos_np[:n], vel_np[:n], ids_np[:n])
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        h2d += n * 28
+        n, _ = sim.update_host(dt, pos_np[:n], vel_np[:n], ids_np[:n])
+        d2h += n * 28
+    ctx.synchronize()
+    te = time.perf_counter() - t0
+    tte = torch.tensor([te], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(tte, op=dist.ReduceOp.MAX)
+    te = float(tte.item())
+
+    if r == 0:
+        mixed, plain = results["mixed"], results["plain"]
+        value = world * args.steps / mixed["t"]
+        # dominant kernel class of the timed mixed region
+        prof = mixed["prof"]
+        dom = max(prof, key=lambda k: prof[k][0])
+        st = mixed["stats"]
+        F = float(np.mean([s["num_fluid_cells"] for s in st]))
+        N = float(np.mean([s["num_particles"] for s in st]))
+        tot_ms, launches = prof[dom]
+        if dom in ("mic0_forward", "mic0_backward"):
+            working = sum(s["sweeps"] for s in st)
+            unit_count = F
+        elif dom in ("matvec", "axpy", "update_search"):
+            working = sum(max(s["cg_iterations"], 0) + s["refinements"] for s in st)
+            unit_count = F
+        else:
+            working = launches
+            unit_count = N
+        bpu = BYTES.get((dom, 1))
+        roof = None
+        if bpu is not None and working > 0:
+            avg_s = tot_ms / 1e3 / working
+            achieved = bpu * unit_count / avg_s / 1e9
+            roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "peak_kind": f"{peak_kind} hbm_gbs",
+                    "bytes_per_launch": bpu * unit_count, "avg_launch_ms": avg_s * 1e3,
+                    "working_launches": working, "traffic": None}
+        breakdown = {k: round(v[0] / args.steps, 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0]) if v[0] > 0}
+        pbreak = {k: round(v[0] / args.steps, 3) for k, v in sorted(plain["prof"].items(), key=lambda kv: -kv[1][0]) if v[0] > 0}
+        plain_rate = world * args.steps / plain["t"]
+        # CPU baseline (rank 0, N = 1 only)
+        cpu = None
+        if world == 1 and not args.no_cpu:
+            iters = int(round(np.mean([max(s["cg_iterations"], 0) for s in plain["stats"]])))
+            tot, parts, wall, ns, nn = cpu_estimate(sc, iters)
+            cpu = {"value": 1.0 / tot, "unit": UNIT, "cores": 1, "kind": "port",
+                   "sample": (f"oracle single-thread: grid-wide stages at full 256^3 size, particle stages on "
+                              f"{ns} of {nn} particles scaled x{nn / ns:.1f}, pressure set-up + per-iteration "
+                              f"cost scaled to {iters} CG iterations (the PLAIN count measured here)"),
+                   "wall_s": round(wall, 1), "stage_seconds": {k: round(v, 4) for k, v in parts.items()}}
+        clocks = mixed["clocks"]
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": mixed["t"] / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (particles, grids, MIC(0)/stencil); f64 dots + refinement residual",
+            "data": "synthetic (seeded scene, no dataset)",
+            "config": {"workload": "slab_spheres 256^3 dx=1/32 + 20 spheres r~U(4,12) cells, 8 ppc, "
+                                   "v~N(0,0.5^2), dt=1/30, 1 substep per step",
+                       "particles": int(st[0]["num_particles"]), "fluid_cells": int(F),
+                       "precision": "mixed", "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (1.3 GB particle state)",
+                       "profiler": "CUDA events around every launch during the timed region"},
+            "plain": {"value": plain_rate, "ms_per_step": plain["t"] / args.steps * 1e3,
+                      "cg_iterations": [s["cg_iterations"] for s in plain["stats"]],
+                      "max_residual": [s["cg_max_residual"] for s in plain["stats"]],
+                      "ms_per_stage": pbreak},
+            "mixed": {"cg_iterations": [s["cg_iterations"] for s in st],
+                      "refinements": [s["refinements"] for s in st],
+                      "max_residual": [s["cg_max_residual"] for s in st],
+                      "ms_per_stage": breakdown},
+            "mixed_over_plain": value / plain_rate,
+            "e2e": {"value": world * args.steps / te, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
+                    "d2h_bytes_per_step": d2h // args.steps},
+            "gpu_launches": int(mixed["launches"]),
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "adjoint": None,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gfs", "reference"], default="gfs")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--ref-cg-iterations", type=int, default=200,
+                    help="CG iterations the reference arm scales its per-iteration cost to")
+    a = ap.parse_args()
+    if a.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    return a
+
+
+if __name__ == "__main__":
+    sys.exit(main(parse()))

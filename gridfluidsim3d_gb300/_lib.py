@@ -43,7 +43,7 @@ class SimParams(ctypes.Structure):
 
 class StepStats(ctypes.Structure):
     _fields_ = [("num_particles", ctypes.c_int64), ("num_fluid_cells", ctypes.c_int64),
-                ("cg_iterations", ctypes.c_int), ("refinements", ctypes.c_int),
+                ("cg_iterations", ctypes.c_int), ("refinements", ctypes.c_int), ("sweeps", ctypes.c_int),
                 ("cg_max_residual", ctypes.c_double), ("pressure_ms", ctypes.c_double),
                 ("step_ms", ctypes.c_double)]
 
@@ -64,6 +64,9 @@ _SIGNATURES = {
     "gfs_ctx_stream": [_P, ctypes.POINTER(_P)],
     "gfs_ctx_device_name": [_P, ctypes.c_char_p, _I],
     "gfs_ctx_launch_count": [_P, ctypes.POINTER(_I64)],
+    "gfs_ctx_profile_enable": [_P, _I],
+    "gfs_ctx_profile_reset": [_P],
+    "gfs_ctx_profile_read": [_P, _I, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_D), ctypes.POINTER(_I64)],
     "gfs_scalar_field_add_point_values": [_P, _P, _P, _I64, _D, _P, _D, _I, _I, _I, _P, _P],
     "gfs_velocity_scalar_field": [_P, _I, _I, _I, _I, _D, _P, _P, _I64, _P, _P],
     "gfs_tricubic_interpolate": [_P, _I, _I, _I, _D, _P, _P, _P, _P, _I64, _P],

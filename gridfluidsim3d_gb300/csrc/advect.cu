@@ -251,6 +251,7 @@ static AdvArgs make_adv(const Grids &g, double dt, double ratio_pic) {
 
 int g2p_advect(Sim *s, double dt) {
     Ctx *ctx = s->ctx;
+    ProfScope prof(ctx, KC_G2P);
     AdvArgs A = make_adv(s->g, dt, s->params.ratio_pic);
     long long nb = s->n_bound;
     if (nb == 0) return GFS_OK;

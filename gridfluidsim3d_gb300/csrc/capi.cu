@@ -27,6 +27,61 @@ void set_error(int code, const char *fmt, ...) {
     va_end(ap);
 }
 
+const char *const kKernelClassNames[KC_COUNT] = {
+    "sort", "classify", "splat", "face_fill", "layers", "extrapolate", "pressure_setup", "mic0_build",
+    "mic0_forward", "mic0_backward", "matvec", "axpy", "update_search", "mixed_refine", "apply_pressure",
+    "g2p_advect"};
+
+cudaEvent_t Profiler::take() {
+    if (!pool.empty()) {
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void Profiler::begin(cudaStream_t st, int cls) {
+    open_cls = cls;
+    open_ev = take();
+    cudaEventRecord(open_ev, st);
+}
+
+void Profiler::end(cudaStream_t st, int cls) {
+    if (open_cls != cls || !open_ev) return;
+    cudaEvent_t b = take();
+    cudaEventRecord(b, st);
+    pending.push_back({cls, open_ev, b});
+    open_ev = nullptr;
+    open_cls = -1;
+}
+
+void Profiler::flush() {
+    for (auto &r : pending) {
+        cudaEventSynchronize(r.b);
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
+            ms[r.cls] += t;
+            count[r.cls] += 1;
+        }
+        pool.push_back(r.a);
+        pool.push_back(r.b);
+    }
+    pending.clear();
+}
+
+void Profiler::reset() {
+    flush();
+    for (int i = 0; i < KC_COUNT; i++) { ms[i] = 0; count[i] = 0; }
+}
+
+Profiler::~Profiler() {
+    for (auto &r : pending) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    for (auto e : pool) cudaEventDestroy(e);
+}
+
 int DevMem::alloc(size_t n) {
     release();
     if (n == 0) n = 16;
@@ -270,6 +325,7 @@ static int sim_step(Sim *s, double dt, gfs_step_stats *stats) {
     if ((rc = sort_particles(s, true))) return rc;
     GFS_CUDA_CHECK(cudaEventRecord(s->ev1, st));
     GFS_CUDA_CHECK(cudaEventSynchronize(s->ev1));
+    if (ctx->prof.on) ctx->prof.flush();
     uint32_t hnum[4];
     GFS_CUDA_CHECK(cudaMemcpy(hnum, s->num.p, sizeof(hnum), cudaMemcpyDeviceToHost));
     float ms = 0.f, pms = 0.f;
@@ -367,6 +423,34 @@ int gfs_ctx_launch_count(gfs_ctx *ctx, int64_t *count) {
     GFS_NONNULL(ctx);
     GFS_NONNULL(count);
     *count = ctx->c.launches;
+    return GFS_OK;
+}
+
+int gfs_ctx_profile_enable(gfs_ctx *ctx, int on) {
+    GFS_NONNULL(ctx);
+    ctx->c.prof.flush();
+    ctx->c.prof.on = on != 0;
+    return GFS_OK;
+}
+
+int gfs_ctx_profile_reset(gfs_ctx *ctx) {
+    GFS_NONNULL(ctx);
+    GFS_CUDA_CHECK(cudaStreamSynchronize(ctx->c.stream));
+    ctx->c.prof.reset();
+    return GFS_OK;
+}
+
+int gfs_ctx_profile_read(gfs_ctx *ctx, int index, const char **name, double *total_ms, int64_t *count) {
+    GFS_NONNULL(ctx);
+    if (index < 0 || index >= KC_COUNT) {
+        set_error(GFS_ERR_INVALID, "profile index %d outside [0, %d)", index, (int)KC_COUNT);
+        return GFS_ERR_INVALID;
+    }
+    GFS_CUDA_CHECK(cudaStreamSynchronize(ctx->c.stream));
+    ctx->c.prof.flush();
+    if (name) *name = kKernelClassNames[index];
+    if (total_ms) *total_ms = ctx->c.prof.ms[index];
+    if (count) *count = ctx->c.prof.count[index];
     return GFS_OK;
 }
 

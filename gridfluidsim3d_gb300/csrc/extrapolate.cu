@@ -42,6 +42,7 @@ __global__ void k_layer_grow(int8_t *__restrict__ layer, const uint8_t *__restri
 
 int build_layers(Sim *s, int num_layers) {
     Ctx *ctx = s->ctx;
+    ProfScope prof(ctx, KC_LAYERS);
     const GridDim &c = s->g.c;
     dim3 grid(grid_blocks(c.nx, 128), c.ny, c.nz);
     k_layer_init<<<grid, 128, 0, ctx->stream>>>(s->layer.as<int8_t>(), s->mat.as<uint8_t>(), c);
@@ -118,6 +119,7 @@ __global__ void __launch_bounds__(128) k_extrap_layer(ExtrapArgs A, const uint8_
 
 int extrapolate_field(Sim *s, float *const fld[3], int num_layers, bool reset) {
     Ctx *ctx = s->ctx;
+    ProfScope prof(ctx, KC_EXTRAP);
     const GridDim &c = s->g.c;
     dim3 block(32, 2, 2);
     dim3 grid(grid_blocks(c.nx + 1, 32), grid_blocks(c.ny + 1, 2), grid_blocks(c.nz + 1, 2));

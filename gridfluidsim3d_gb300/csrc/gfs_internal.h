@@ -3,6 +3,7 @@
 
 #include <cstdarg>
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "gfs.h"
@@ -23,12 +24,46 @@ struct DevMem {
     template <class T> T *as() const { return static_cast<T *>(p); }
 };
 
+// Kernel classes timed by the optional profiler (CUDA events on the stream).
+enum KernelClass {
+    KC_SORT = 0, KC_CLASSIFY, KC_SPLAT, KC_FILL, KC_LAYERS, KC_EXTRAP, KC_PS_SETUP, KC_PRECON,
+    KC_SWEEP_FWD, KC_SWEEP_BWD, KC_MATVEC, KC_AXPY, KC_UPDATE_S, KC_MIXED_AUX, KC_APPLY, KC_G2P,
+    KC_COUNT
+};
+extern const char *const kKernelClassNames[KC_COUNT];
+
+struct Profiler {
+    bool on = false;
+    struct Rec { int cls; cudaEvent_t a, b; };
+    std::vector<Rec> pending;
+    std::vector<cudaEvent_t> pool;
+    double ms[KC_COUNT] = {0};
+    long long count[KC_COUNT] = {0};
+    int open_cls = -1;
+    cudaEvent_t open_ev = nullptr;
+    cudaEvent_t take();
+    void begin(cudaStream_t st, int cls);
+    void end(cudaStream_t st, int cls);
+    void flush();     // waits for the recorded events and accumulates their times
+    void reset();
+    ~Profiler();
+};
+
 struct Ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     int64_t launches = 0;
     char device_name[256] = {0};
+    Profiler prof;
+};
+
+// Scoped timing of one kernel class (no-op unless the profiler is on).
+struct ProfScope {
+    Ctx *c;
+    int cls;
+    ProfScope(Ctx *ctx, int k) : c(ctx), cls(k) { if (c->prof.on) c->prof.begin(c->stream, cls); }
+    ~ProfScope() { if (c->prof.on) c->prof.end(c->stream, cls); }
 };
 
 // Controls of the pressure solve, kept in device memory so that the CG loop
@@ -49,18 +84,23 @@ struct PsCtrl {
     unsigned err;                // GFS_DEV_ERR_* bits
     unsigned tickets[4];         // last-block-done tickets of fused reductions
     unsigned sweep_ticket[3];    // dispatch tickets of the wavefront kernels (fwd, bwd, precon)
+    unsigned epoch;              // tag of the current wavefront's exchange words
 };
 
-// Dense padded pressure workspace over the cell grid.
+// Pressure workspace.  flags / b / p are dense over the padded cell grid; the
+// solver's vectors use the skewed block layout of pressure.cu (skew_size slots).
 struct PressureWs {
     GridDim c{};
     int nbj = 0, nbk = 0;        // wavefront block grid
-    DevMem flags;                // uint8
-    DevMem b, p, r, z, s, As, q, precon;            // FP64
-    DevMem r32, z32, s32, As32, q32, e32, precon32; // FP32 (mixed)
+    long long skew_size = 0;
+    DevMem flags, b, p;          // padded cell layout: uint8, FP64, FP64 (the solution)
+    DevMem fsk;                  // skewed flags
+    DevMem bsk, psk, r, z, s, As, q, precon;        // FP64, skewed
+    DevMem r32, z32, s32, As32, q32, e32, precon32; // FP32 (mixed), skewed
     DevMem partials;             // double per block
     DevMem ctrl;                 // PsCtrl
-    DevMem progress;             // unsigned per wavefront block x 3 kinds
+    DevMem xch;                  // block-boundary exchange words of the wavefronts
+    DevMem nbstd, nbsk;          // MIC(0) neighbour bits, padded cell and skewed layouts
     size_t nblocks_red = 0;      // blocks of the reduction kernels
     long long allocated_for = -1;
     bool mixed_alloc = false;

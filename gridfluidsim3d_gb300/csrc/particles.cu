@@ -227,6 +227,7 @@ int exclusive_scan_u32(Ctx *ctx, uint32_t *in, uint32_t *out, long long n, uint3
 
 int sort_particles(Sim *s, bool /*remove_solid*/) {
     Ctx *ctx = s->ctx;
+    ProfScope prof(ctx, KC_SORT);
     cudaStream_t st = ctx->stream;
     const GridDim &c = s->g.c;
     long long ncells = (long long)c.nx * c.ny * c.nz;
@@ -308,6 +309,7 @@ __global__ void k_classify(uint8_t *__restrict__ mat, GridDim c, const uint32_t 
 
 int classify_cells(Sim *s) {
     Ctx *ctx = s->ctx;
+    ProfScope prof(ctx, KC_CLASSIFY);
     const GridDim &c = s->g.c;
     uint32_t *num = s->num.as<uint32_t>();
     GFS_CUDA_CHECK(cudaMemsetAsync(num + 2, 0, sizeof(uint32_t), ctx->stream));

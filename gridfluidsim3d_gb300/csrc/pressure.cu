@@ -1,29 +1,21 @@
 // pressure.cu -- MICCG(0) pressure projection (PressureSolver, pressuresolver.cpp)
 // and the pressure update of the MAC field.
 //
-// Layout: every vector is dense over the padded cell grid (GridDim), zero on
-// non-fluid cells and on the halo.  A one-byte flag per cell holds "fluid" and
-// the MatrixCell diagonal (number of non-solid neighbours).  With zeros off the
-// fluid set, the reference's keymap lookups (found -> value, not found -> 0)
-// become plain 7-point stencils, and every per-cell formula keeps the
-// reference's operation order; the FP64 (PLAIN) kernels use explicitly rounded
-// intrinsics (no FMA contraction), so the preconditioner, the stencil and the
-// triangular solves reproduce the reference's doubles bit for bit.  Only the
-// dot products differ (parallel summation order).
-//
-// MIC(0) triangular solves.  The forward solve L q = r and the build of the
-// preconditioner are recurrences over i-1, j-1, k-1; the backward solve over
-// i+1, j+1, k+1 (pressuresolver.cpp:246-386).  A cell depends only on cells of
-// a lower i+j+k plane, so a wavefront reproduces the sequential result.  Each
-// CTA owns a BJ x BK block of (j, k) pencils, one thread per pencil, and walks
-// i: at step s thread (jl, kl) updates cell i = s - jl - kl.  The j-1 / k-1
-// neighbours were produced by the adjacent threads at step s-1 (shared-memory
-// exchange, one barrier per step), i-1 by the thread itself.  Neighbouring
-// CTAs exchange their boundary rows through global memory: a CTA publishes how
-// many steps it has completed (st.release) and a consumer waits (ld.acquire,
-// bounded spin) only when it has caught up with its producer, so the CTAs form
-// a pipeline over the (j, k) block grid.  CTAs take dispatch tickets in
-// dependency order, so every CTA they wait for is already resident.
+// Vector layout.  The solver's vectors live in a "skewed" layout built for the
+// MIC(0) triangular solves.  The forward solve L q = r and the preconditioner
+// build are recurrences over i-1, j-1, k-1, the backward solve over i+1, j+1,
+// k+1 (pressuresolver.cpp:246-386).  A cell depends only on cells of a lower
+// i+j+k plane, so a wavefront reproduces the sequential result.  Each CTA owns
+// one block: SBJ*SBK threads, one per pencil, walk the block's planes (step t
+// handles plane t forwards, plane S-1-t backwards).  The j / k neighbours were
+// produced by the adjacent threads one step earlier (shared-memory exchange,
+// one barrier per step), the i neighbour by the thread itself.  Per-cell
+// inputs are prefetched P steps ahead into registers.  Blocks hand their edge
+// values to the downstream blocks through tagged 64-bit exchange words (value
+// bits | sweep epoch): a consumer prefetches the word it will need P steps
+// later and only re-reads it (bounded) if the tag is not yet this sweep's, so
+// no fence or progress counter sits on the per-step path.  CTAs take dispatch
+// tickets in dependency order, so every CTA they wait for is already resident.
 //
 // The CG loop runs on the device: each kernel first checks a device "done"
 // flag, reductions finish in the last CTA to arrive (fixed order, so results
@@ -50,16 +42,28 @@ template <> struct Ar<float> {
 
 template <class T> __device__ __forceinline__ T ldcg(const T *p) { return __ldcg(p); }
 
+__device__ __forceinline__ unsigned ld_acquire_cta_shared(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.cta.shared.u32 %0, [%1];" : "=r"(v) : "r"((unsigned)__cvta_generic_to_shared(p)) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_cta_shared(unsigned *p, unsigned v) {
+    asm volatile("st.release.cta.shared.u32 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(p)), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void named_barrier(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 #define RED_THREADS 256
 
 template <int OP>  // 0 = sum, 1 = max
 __device__ __forceinline__ double block_reduce(double v) {
     __shared__ double sh[32];
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
     int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
-    lane = tid & 31;
-    warp = tid >> 5;
+    int lane = tid & 31, warp = tid >> 5;
     for (int o = 16; o > 0; o >>= 1) {
         double y = __shfl_down_sync(0xffffffffu, v, o);
         v = OP == 0 ? v + y : fmax(v, y);
@@ -67,7 +71,7 @@ __device__ __forceinline__ double block_reduce(double v) {
     if (lane == 0) sh[warp] = v;
     __syncthreads();
     if (warp == 0) {
-        v = lane < nw ? sh[lane] : (OP == 0 ? 0.0 : 0.0);
+        v = lane < nw ? sh[lane] : 0.0;
         for (int o = 16; o > 0; o >>= 1) {
             double y = __shfl_down_sync(0xffffffffu, v, o);
             v = OP == 0 ? v + y : fmax(v, y);
@@ -97,7 +101,6 @@ __device__ __forceinline__ bool finish_reduce(double part, double *partials, uns
     if (!last) return false;
     __threadfence();
     double acc = 0.0;
-    // fixed assignment of partials to threads, fixed tree: deterministic
     for (unsigned q = tid; q < nblocks; q += nthr) {
         double v = __ldcg(partials + q);
         acc = OP == 0 ? acc + v : fmax(acc, v);
@@ -110,6 +113,43 @@ __device__ __forceinline__ bool finish_reduce(double part, double *partials, uns
     return true;
 }
 
+// ---------------------------------------------------------- skewed layout
+
+static constexpr int SBJ = 16, SBK = 16, SPLANE = SBJ * SBK;
+
+struct Skew {
+    int nx, ny, nz, nbj, nbk, S;
+    long long size;
+    __host__ __device__ __forceinline__ long long base(int bj, int bk) const {
+        return ((long long)bk * nbj + bj) * (long long)S * SPLANE;
+    }
+    __host__ __device__ __forceinline__ long long slot(int bj, int bk, int s, int jl, int kl) const {
+        return base(bj, bk) + (long long)s * SPLANE + kl * SBJ + jl;
+    }
+    // slot -> block, plane and pencil position
+    __device__ __forceinline__ void decode(long long q, int &bj, int &bk, int &s, int &jl, int &kl) const {
+        long long per = (long long)S * SPLANE;
+        long long blk = q / per;
+        int rem = (int)(q - blk * per);
+        s = rem / SPLANE;
+        int w = rem - s * SPLANE;
+        kl = w / SBJ;
+        jl = w - kl * SBJ;
+        bk = (int)(blk / nbj);
+        bj = (int)(blk - (long long)bk * nbj);
+    }
+};
+
+static Skew make_skew(const GridDim &c) {
+    Skew K;
+    K.nx = c.nx; K.ny = c.ny; K.nz = c.nz;
+    K.nbj = (c.ny + SBJ - 1) / SBJ;
+    K.nbk = (c.nz + SBK - 1) / SBK;
+    K.S = c.nx + SBJ + SBK - 2;
+    K.size = (long long)K.nbj * K.nbk * K.S * SPLANE;
+    return K;
+}
+
 // ------------------------------------------------------------------ setup
 
 struct SetupArgs {
@@ -120,20 +160,21 @@ struct SetupArgs {
 };
 
 // _calculateNegativeDivergenceVector (pressuresolver.cpp:162-208) and
-// _calculateMatrixCoefficients (:222-244) for one cell; also resets p, r, s.
+// _calculateMatrixCoefficients (:222-244) for one cell, in the padded cell layout.
 __global__ void __launch_bounds__(RED_THREADS) k_ps_setup(SetupArgs A, const uint8_t *__restrict__ mat,
                                                           const float *__restrict__ u, const float *__restrict__ v,
                                                           const float *__restrict__ w, uint8_t *__restrict__ flags,
-                                                          double *__restrict__ b, double *__restrict__ r,
-                                                          double *__restrict__ p, double *__restrict__ s,
-                                                          double *__restrict__ partials, PsCtrl *ctrl) {
+                                                          double *__restrict__ b, double *__restrict__ partials,
+                                                          PsCtrl *ctrl) {
     const GridDim &c = A.c;
+    const unsigned plane = (unsigned)c.sx * (unsigned)c.sy;
     double mx = 0.0;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < c.size;
          e += (long long)gridDim.x * blockDim.x) {
-        long long kq = e / ((long long)c.sx * c.sy);
-        long long rem = e - kq * (long long)c.sx * c.sy;
-        int k = (int)kq - GFS_PAD, j = (int)(rem / c.sx) - GFS_PAD, i = (int)(rem % c.sx) - GFS_PAD;
+        unsigned ue = (unsigned)e;
+        int k = (int)(ue / plane) - GFS_PAD;
+        unsigned rem = ue % plane;
+        int j = (int)(rem / (unsigned)c.sx) - GFS_PAD, i = (int)(rem % (unsigned)c.sx) - GFS_PAD;
         uint8_t fl = 0;
         double bv = 0.0;
         if (c.in(i, j, k) && mat[e] == GFS_FLUID) {
@@ -158,9 +199,6 @@ __global__ void __launch_bounds__(RED_THREADS) k_ps_setup(SetupArgs A, const uin
         }
         flags[e] = fl;
         b[e] = bv;
-        r[e] = bv;
-        p[e] = 0.0;
-        s[e] = 0.0;
     }
     double part = block_reduce<1>(mx);
     double res;
@@ -181,201 +219,460 @@ __global__ void __launch_bounds__(RED_THREADS) k_ps_setup(SetupArgs A, const uin
     }
 }
 
+// padded cell layout -> skewed layout: flags, b; r = b, p = 0, s = 0
+__global__ void __launch_bounds__(RED_THREADS) k_to_skew(Skew K, GridDim c, const uint8_t *__restrict__ flags,
+                                                         const double *__restrict__ b,
+                                                         const uint16_t *__restrict__ nbits,
+                                                         uint8_t *__restrict__ fsk, uint16_t *__restrict__ nbsk,
+                                                         double *__restrict__ bsk, double *__restrict__ rsk,
+                                                         double *__restrict__ psk, double *__restrict__ ssk) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < K.size;
+         q += (long long)gridDim.x * blockDim.x) {
+        int bj, bk, s, jl, kl;
+        K.decode(q, bj, bk, s, jl, kl);
+        int i = s - jl - kl, j = bj * SBJ + jl, k = bk * SBK + kl;
+        uint8_t fl = 0;
+        uint16_t nb = 0;
+        double bv = 0.0;
+        if (c.in(i, j, k)) {
+            long long e = c.at(i, j, k);
+            fl = flags[e];
+            bv = b[e];
+            nb = nbits[e];
+        }
+        fsk[q] = fl;
+        nbsk[q] = nb;
+        bsk[q] = bv;
+        rsk[q] = bv;
+        psk[q] = 0.0;
+        ssk[q] = 0.0;
+    }
+}
+
+// skewed pressure -> padded cell layout (0 off the fluid set)
+__global__ void k_from_skew(Skew K, GridDim c, const uint8_t *__restrict__ flags, const double *__restrict__ psk,
+                            double *__restrict__ p) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y, k = blockIdx.z;
+    if (i >= c.nx) return;
+    long long e = c.at(i, j, k);
+    double v = 0.0;
+    if (flags[e] & GFS_PF_FLUID) {
+        int bj = j / SBJ, bk = k / SBK, jl = j - bj * SBJ, kl = k - bk * SBK;
+        v = psk[K.slot(bj, bk, i + jl + kl, jl, kl)];
+    }
+    p[e] = v;
+}
+
 // ------------------------------------------------------------ wavefronts
 
 enum { SW_PRECON = 0, SW_FWD = 1, SW_BWD = 2 };
 
 template <class T>
 struct SweepArgs {
-    GridDim c;
-    int nbj, nbk, S;
-    const uint8_t *flags;
-    const T *in;          // FWD: r, BWD: q
-    T *out;               // FWD: q, BWD: z, PRECON: precon (double)
-    const T *precon;      // FWD/BWD
-    const T *rdot;        // BWD: r, for dot(z, r)
-    float *out32;         // PRECON: float copy of precon (MIXED)
+    Skew K;
+    GridDim c;               // padded cell layout (neighbour flags of the MIC(0) build)
+    const uint8_t *fsk;      // skewed flags
+    const uint8_t *fstd;     // padded-layout flags
+    const T *in;             // FWD: r, BWD: q
+    T *out;                  // FWD: q, BWD: z, PRECON: precon (double)
+    const T *precon;         // FWD/BWD
+    const T *rdot;           // BWD: r, for dot(z, r)
+    float *out32;            // PRECON: float copy of precon (MIXED)
     T negscale;
     double scale, dnegscale;
-    unsigned *progress;   // nbj * nbk
-    unsigned *ticket;     // dispatch ticket
+    unsigned long long *xch; // block-boundary exchange words
+    const uint16_t *nbits;   // PRECON: skewed MIC(0) neighbour bits
+    unsigned *ticket;        // dispatch ticket
     unsigned *done_ticket;
     double *partials;
     PsCtrl *ctrl;
-    int init;             // BWD: first solve of a CG run (sets sigma, no beta)
+    int init;                // BWD: first solve of a CG run (sets sigma, no beta)
 };
 
-__device__ __forceinline__ void wait_progress(const unsigned *p, unsigned need, unsigned &cached,
-                                              bool &timed_out, PsCtrl *ctrl) {
-    if (cached >= need || timed_out) return;
-    int spins = 0;
-    while ((cached = ld_acquire_u32(p)) < need) {
-        if (++spins > GFS_SPIN_LIMIT) {
-            atomicOr(&ctrl->err, GFS_DEV_ERR_TIMEOUT);
-            timed_out = true;
-            return;
-        }
-    }
+// Fluid bits of the neighbours the MIC(0) diagonal needs, packed:
+//   0 i-1, 1 j-1, 2 k-1, 3 (i-1,j+1), 4 (i-1,k+1), 5 (i+1,j-1), 6 (j-1,k+1),
+//   7 (i+1,k-1), 8 (j+1,k-1).
+__device__ __forceinline__ unsigned mic0_neighbour_bits(const uint8_t *__restrict__ flags, const GridDim &c,
+                                                        long long e) {
+    const long long sx = 1, sy = c.sx, sz = (long long)c.sx * c.sy;
+    const long long off[9] = {-sx, -sy, -sz, -sx + sy, -sx + sz, sx - sy, -sy + sz, sx - sz, sy - sz};
+    unsigned bits = 0;
+#pragma unroll
+    for (int q = 0; q < 9; q++) bits |= (flags[e + off[q]] & GFS_PF_FLUID) ? (1u << q) : 0u;
+    return bits;
+}
+
+// neighbour bits of every fluid cell, padded cell layout (input of the MIC(0) build)
+__global__ void k_nbits(GridDim c, const uint8_t *__restrict__ flags, uint16_t *__restrict__ nbits) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y, k = blockIdx.z;
+    if (i >= c.nx) return;
+    long long e = c.at(i, j, k);
+    nbits[e] = (flags[e] & GFS_PF_FLUID) ? (uint16_t)mic0_neighbour_bits(flags, c, e) : (uint16_t)0;
 }
 
 // MIC(0) diagonal for one fluid cell (pressuresolver.cpp:255-301).  pim1/pjm1/pkm1
 // are the preconditioner values of the i-1, j-1, k-1 neighbours (0 if not fluid).
-__device__ __forceinline__ double mic0_precon(const uint8_t *__restrict__ flags, const GridDim &c,
-                                              long long e, uint8_t fl, double pim1, double pjm1,
-                                              double pkm1, double scale, double negscale) {
-    const double tau = 0.97, sigma = 0.25;
-    long long sx = 1, sy = c.sx, sz = (long long)c.sx * c.sy;
-    bool fim1 = flags[e - sx] & GFS_PF_FLUID, fjm1 = flags[e - sy] & GFS_PF_FLUID,
-         fkm1 = flags[e - sz] & GFS_PF_FLUID;
+// In double it reproduces the reference's arithmetic exactly; the MIXED solver
+// builds its FP32 preconditioner with the same formula in float.
+template <class T>
+__device__ __forceinline__ T mic0_precon(unsigned nb, uint8_t fl, T pim1, T pjm1, T pkm1, T scale, T negscale) {
+    using Op = Ar<T>;
+    const T tau = (T)0.97, sigma = (T)0.25, zero = T(0), one = T(1);
+    bool fim1 = nb & 1u, fjm1 = nb & 2u, fkm1 = nb & 4u;
     // MatrixCell plus flags of the lower neighbours: A[n].plusX = fluid(n + e_X)
-    double plusi_im1 = fim1 ? __dmul_rn(1.0, negscale) : 0.0;
-    double plusj_im1 = fim1 ? __dmul_rn((double)((flags[e - sx + sy] & GFS_PF_FLUID) ? 1 : 0), negscale) : 0.0;
-    double plusk_im1 = fim1 ? __dmul_rn((double)((flags[e - sx + sz] & GFS_PF_FLUID) ? 1 : 0), negscale) : 0.0;
-    double plusi_jm1 = fjm1 ? __dmul_rn((double)((flags[e - sy + sx] & GFS_PF_FLUID) ? 1 : 0), negscale) : 0.0;
-    double plusj_jm1 = fjm1 ? __dmul_rn(1.0, negscale) : 0.0;
-    double plusk_jm1 = fjm1 ? __dmul_rn((double)((flags[e - sy + sz] & GFS_PF_FLUID) ? 1 : 0), negscale) : 0.0;
-    double plusi_km1 = fkm1 ? __dmul_rn((double)((flags[e - sz + sx] & GFS_PF_FLUID) ? 1 : 0), negscale) : 0.0;
-    double plusj_km1 = fkm1 ? __dmul_rn((double)((flags[e - sz + sy] & GFS_PF_FLUID) ? 1 : 0), negscale) : 0.0;
-    double plusk_km1 = fkm1 ? __dmul_rn(1.0, negscale) : 0.0;
-    double precon_im1 = fim1 ? pim1 : 0.0, precon_jm1 = fjm1 ? pjm1 : 0.0, precon_km1 = fkm1 ? pkm1 : 0.0;
-    double diag = __dmul_rn((double)(fl >> 1), scale);
-    double v1 = __dmul_rn(plusi_im1, precon_im1);
-    double v2 = __dmul_rn(plusj_jm1, precon_jm1);
-    double v3 = __dmul_rn(plusk_km1, precon_km1);
-    double v4 = __dmul_rn(precon_im1, precon_im1);
-    double v5 = __dmul_rn(precon_jm1, precon_jm1);
-    double v6 = __dmul_rn(precon_km1, precon_km1);
-    double ta = __dmul_rn(__dmul_rn(plusi_im1, __dadd_rn(plusj_im1, plusk_im1)), v4);
-    double tb = __dmul_rn(__dmul_rn(plusj_jm1, __dadd_rn(plusi_jm1, plusk_jm1)), v5);
-    double tc = __dmul_rn(__dmul_rn(plusk_km1, __dadd_rn(plusi_km1, plusj_km1)), v6);
-    double ee = __dsub_rn(__dsub_rn(__dsub_rn(__dsub_rn(diag, __dmul_rn(v1, v1)), __dmul_rn(v2, v2)),
-                                    __dmul_rn(v3, v3)),
-                          __dmul_rn(tau, __dadd_rn(__dadd_rn(ta, tb), tc)));
-    if (ee < __dmul_rn(sigma, diag)) ee = diag;
-    return fabs(ee) > 10e-9 ? __ddiv_rn(1.0, __dsqrt_rn(ee)) : 0.0;
+    T plusi_im1 = fim1 ? Op::mul(one, negscale) : zero;
+    T plusj_im1 = fim1 ? Op::mul((nb & 8u) ? one : zero, negscale) : zero;
+    T plusk_im1 = fim1 ? Op::mul((nb & 16u) ? one : zero, negscale) : zero;
+    T plusi_jm1 = fjm1 ? Op::mul((nb & 32u) ? one : zero, negscale) : zero;
+    T plusj_jm1 = fjm1 ? Op::mul(one, negscale) : zero;
+    T plusk_jm1 = fjm1 ? Op::mul((nb & 64u) ? one : zero, negscale) : zero;
+    T plusi_km1 = fkm1 ? Op::mul((nb & 128u) ? one : zero, negscale) : zero;
+    T plusj_km1 = fkm1 ? Op::mul((nb & 256u) ? one : zero, negscale) : zero;
+    T plusk_km1 = fkm1 ? Op::mul(one, negscale) : zero;
+    T precon_im1 = fim1 ? pim1 : zero, precon_jm1 = fjm1 ? pjm1 : zero, precon_km1 = fkm1 ? pkm1 : zero;
+    T diag = Op::mul((T)(fl >> 1), scale);
+    T v1 = Op::mul(plusi_im1, precon_im1);
+    T v2 = Op::mul(plusj_jm1, precon_jm1);
+    T v3 = Op::mul(plusk_km1, precon_km1);
+    T v4 = Op::mul(precon_im1, precon_im1);
+    T v5 = Op::mul(precon_jm1, precon_jm1);
+    T v6 = Op::mul(precon_km1, precon_km1);
+    T ta = Op::mul(Op::mul(plusi_im1, Op::add(plusj_im1, plusk_im1)), v4);
+    T tb = Op::mul(Op::mul(plusj_jm1, Op::add(plusi_jm1, plusk_jm1)), v5);
+    T tc = Op::mul(Op::mul(plusk_km1, Op::add(plusi_km1, plusj_km1)), v6);
+    T ee = Op::sub(Op::sub(Op::sub(Op::sub(diag, Op::mul(v1, v1)), Op::mul(v2, v2)), Op::mul(v3, v3)),
+                   Op::mul(tau, Op::add(Op::add(ta, tb), tc)));
+    if (ee < Op::mul(sigma, diag)) ee = diag;
+    if (!(fabs((double)ee) > 10e-9)) return zero;
+    if (sizeof(T) == 8) return (T)__ddiv_rn(1.0, __dsqrt_rn((double)ee));
+    return (T)(1.0f / sqrtf((float)ee));
 }
 
-template <class T, int BJ, int BK, int MODE>
-__global__ void __launch_bounds__(BJ *BK) k_sweep(SweepArgs<T> A) {
-    using Op = Ar<T>;
-    if (A.ctrl->done) return;
-    __shared__ T xb[2][BK][BJ];
-    __shared__ unsigned sh_ticket;
-    const int tid = threadIdx.x;
-    const int jl = tid % BJ, kl = tid / BJ;
-    if (tid == 0) sh_ticket = atomicAdd(A.ticket, 1u);
-    __syncthreads();
-    const unsigned t = sh_ticket;
-    int bj, bk;
-    if (MODE == SW_BWD) {
-        bj = A.nbj - 1 - (int)(t % A.nbj);
-        bk = A.nbk - 1 - (int)(t / A.nbj);
-    } else {
-        bj = (int)(t % A.nbj);
-        bk = (int)(t / A.nbj);
-    }
-    const GridDim &c = A.c;
-    const int j = bj * BJ + jl, k = bk * BK + kl;
-    const bool valid = j < c.ny && k < c.nz;
-    const long long sy = c.sx, sz = (long long)c.sx * c.sy;
-    const int S = A.S;
+#define SWEEP_THREADS SPLANE
+#define XCH_PER_PLANE (SBJ + SBK)   // exchange entries per block plane: j edge (by kl), k edge (by jl)
 
-    // producers of this block's boundary rows
-    const unsigned *prod_j = nullptr, *prod_k = nullptr;
-    if (MODE == SW_BWD) {
-        if (bj + 1 < A.nbj) prod_j = A.progress + (bk * A.nbj + bj + 1);
-        if (bk + 1 < A.nbk) prod_k = A.progress + ((bk + 1) * A.nbj + bj);
-    } else {
-        if (bj > 0) prod_j = A.progress + (bk * A.nbj + bj - 1);
-        if (bk > 0) prod_k = A.progress + ((bk - 1) * A.nbj + bj);
+// Block-boundary exchange.  The threads on a block's downstream j / k edge write
+// the value each of their cells hands to the neighbouring block into an
+// exchange buffer as 64-bit words (32 value bits | 32-bit sweep epoch).  A
+// 64-bit aligned store is single-copy atomic, so a consumer that reads a word
+// whose tag equals the current epoch holds the producer's value for this sweep:
+// no progress counters and no memory fences are needed.  FP64 values travel as
+// two tagged words.
+template <class T> struct Xch;
+template <> struct Xch<float> {
+    static constexpr int W = 1;
+    static __device__ __forceinline__ void put(unsigned long long *p, float v, unsigned tag) {
+        unsigned long long w = ((unsigned long long)tag << 32) | (unsigned long long)__float_as_uint(v);
+        __stcg(p, w);
     }
-    unsigned *mine = A.progress + (bk * A.nbj + bj);
-    unsigned cj = 0, ck = 0;
+    static __device__ __forceinline__ void fetch(const unsigned long long *p, unsigned long long w[1]) {
+        w[0] = __ldcg(p);
+    }
+    static __device__ __forceinline__ bool ready(const unsigned long long w[1], unsigned tag) {
+        return (unsigned)(w[0] >> 32) == tag;
+    }
+    static __device__ __forceinline__ float value(const unsigned long long w[1]) {
+        return __uint_as_float((unsigned)(w[0] & 0xFFFFFFFFull));
+    }
+};
+template <> struct Xch<double> {
+    static constexpr int W = 2;
+    static __device__ __forceinline__ void put(unsigned long long *p, double v, unsigned tag) {
+        unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+        __stcg(p, ((unsigned long long)tag << 32) | (bits & 0xFFFFFFFFull));
+        __stcg(p + 1, ((unsigned long long)tag << 32) | (bits >> 32));
+    }
+    static __device__ __forceinline__ void fetch(const unsigned long long *p, unsigned long long w[2]) {
+        w[0] = __ldcg(p);
+        w[1] = __ldcg(p + 1);
+    }
+    static __device__ __forceinline__ bool ready(const unsigned long long w[2], unsigned tag) {
+        return (unsigned)(w[0] >> 32) == tag && (unsigned)(w[1] >> 32) == tag;
+    }
+    static __device__ __forceinline__ double value(const unsigned long long w[2]) {
+        return __longlong_as_double((long long)((w[0] & 0xFFFFFFFFull) | (w[1] << 32)));
+    }
+};
+
+// Take a prefetched exchange word, re-reading it (bounded) until it carries this sweep's tag.
+template <class T>
+__device__ __forceinline__ T xch_take(unsigned long long w[], const unsigned long long *src, unsigned tag,
+                                      PsCtrl *ctrl, bool &timed_out) {
+    if (!Xch<T>::ready(w, tag) && !timed_out) {
+        int spins = 0;
+        do {
+            Xch<T>::fetch(src, w);
+            if (++spins > GFS_SPIN_LIMIT) {
+                atomicOr(&ctrl->err, GFS_DEV_ERR_TIMEOUT);
+                timed_out = true;
+                break;
+            }
+        } while (!Xch<T>::ready(w, tag));
+    }
+    return Xch<T>::value(w);
+}
+
+// Compensated (double-float) accumulation: s + c tracks a running sum with
+// about twice float precision (Knuth's TwoSum), so the FP32 kernels form their
+// dot-product partials without FP64 arithmetic.
+struct Acc2f {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        float t = s + x;
+        float bp = t - s;
+        float err = (s - (t - bp)) + (x - bp);
+        s = t;
+        c += err;
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+// ---- TMA bulk copies into a shared-memory ring, completion tracked by mbarriers
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// 1-D bulk copy global -> shared (16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void tma_load_1d(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+// Exchange words are read with an in-place L2 load (asm volatile keeps it where it is written).
+__device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.global.cg.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// In-place loads for the wavefront's prefetch ring: asm volatile keeps each load
+// where it is written (P steps before its use), so its latency overlaps the
+// intervening steps instead of sitting on the step's critical path.
+__device__ __forceinline__ float ld_nc(const float *p) {
+    float v;
+    asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ double ld_nc(const double *p) {
+    double v;
+    asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ unsigned ld_nc_u8(const uint8_t *p) {
+    unsigned v;
+    asm volatile("ld.global.nc.u8 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ unsigned ld_nc_u16(const uint16_t *p) {
+    unsigned short v;
+    asm volatile("ld.global.nc.u16 %0, [%1];" : "=h"(v) : "l"(p));
+    return v;
+}
+
+// Per-thread asynchronous copies (cp.async) into the shared-memory ring: one
+// commit group per step, waited for P-1 groups later, so the copy of step st+P
+// overlaps P steps of the recurrence without holding any register scoreboard.
+template <int N>
+__device__ __forceinline__ void cp_async(void *dst, const void *src, bool pred) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(smem_addr(dst)), "l"(src), "n"(N),
+                 "r"(pred ? N : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+template <class T, int MODE, int P, int PE>
+__global__ void __launch_bounds__(SWEEP_THREADS, 1) k_sweep(SweepArgs<T> A) {
+    using Op = Ar<T>;
+    using X = Xch<T>;
+    constexpr bool bwd = MODE == SW_BWD;
+    constexpr long long PS = bwd ? -(long long)SPLANE : (long long)SPLANE;   // slot advance per step
+    constexpr long long XP = (long long)XCH_PER_PLANE * X::W;               // exchange words per plane
+    constexpr long long XS = bwd ? -XP : XP;                                // exchange advance per step
+    __shared__ T xb[2][SBK][SBJ];
+    // ring of P steps per input (FWD: r, precon; BWD: q, precon, r); each thread owns column tid
+    __shared__ __align__(16) T ring[(MODE == SW_PRECON) ? 1 : (MODE == SW_BWD ? 3 : 2)][P][SPLANE];
+    __shared__ unsigned sh_ticket, sh_epoch;
+    if (A.ctrl->done) return;
+    const int tid = threadIdx.x;
+    const Skew &K = A.K;
+    const int S = K.S;
+    if (tid == 0) {
+        sh_ticket = atomicAdd(A.ticket, 1u);
+        sh_epoch = A.ctrl->epoch;
+    }
+    __syncthreads();
+    const unsigned t = sh_ticket, tag = sh_epoch;
+    int bj = (int)(t % K.nbj), bk = (int)(t / K.nbj);
+    if (bwd) {
+        bj = K.nbj - 1 - bj;
+        bk = K.nbk - 1 - bk;
+    }
+    const int pbj = bwd ? bj + 1 : bj - 1, pbk = bwd ? bk + 1 : bk - 1;
+    const bool has_pj = pbj >= 0 && pbj < K.nbj, has_pk = pbk >= 0 && pbk < K.nbk;
     bool timed_out = false;
 
-    if (tid == 0) {
-        if (prod_j) wait_progress(prod_j, min(BJ, S), cj, timed_out, A.ctrl);
-        if (prod_k) wait_progress(prod_k, min(BK, S), ck, timed_out, A.ctrl);
-    }
-    __syncthreads();
+    const int jl = tid % SBJ, kl = tid / SBJ;
+    const int j = bj * SBJ + jl, k = bk * SBK + kl;
+    const bool valid = j < K.ny && k < K.nz;
+    const int xj = bwd ? jl + 1 : jl - 1, xk = bwd ? kl + 1 : kl - 1;
+    const bool at_j = bwd ? jl == SBJ - 1 : jl == 0;                // on the upstream j edge
+    const bool at_k = bwd ? kl == SBK - 1 : kl == 0;
+    const bool in_j = at_j && has_pj, in_k = at_k && has_pk;        // read a producer block
+    const bool out_j = bwd ? jl == 0 : jl == SBJ - 1;               // write for the j consumer
+    const bool out_k = bwd ? kl == 0 : kl == SBK - 1;
+    // step st handles plane S-1-st (backward) or st (forward); the cell exists for st in [st_lo, st_hi)
+    const int st_lo = valid ? (bwd ? S - K.nx - jl - kl : jl + kl) : S;
+    const int st_hi = valid ? st_lo + K.nx : S;
+    const long long q0 = K.base(bj, bk) + kl * SBJ + jl + (bwd ? (long long)(S - 1) * SPLANE : 0);
+    const long long xblock = (long long)S * XP;
+    const long long xo0 = (long long)(bk * K.nbj + bj) * xblock + (bwd ? (long long)(S - 1) * XP : 0);
+    const long long xj0 = has_pj ? (long long)(bk * K.nbj + pbj) * xblock +
+                                       (bwd ? (long long)(S - 1 - (SBJ - 1)) : (long long)(SBJ - 1)) * XP +
+                                       (long long)kl * X::W
+                                 : 0;
+    const long long xk0 = has_pk ? (long long)(pbk * K.nbj + bj) * xblock +
+                                       (bwd ? (long long)(S - 1 - (SBK - 1)) : (long long)(SBK - 1)) * XP +
+                                       (long long)(SBJ + jl) * X::W
+                                 : 0;
+    // per-thread pointers at step 0 (every step moves them by PS slots)
+    const T *pa = MODE == SW_PRECON ? nullptr : A.in + q0;        // FWD r, BWD q
+    const T *pb = MODE == SW_PRECON ? nullptr : A.precon + q0;
+    const T *pc_ = MODE == SW_BWD ? A.rdot + q0 : nullptr;        // BWD r
+    const uint8_t *pf = MODE == SW_PRECON ? A.fsk + q0 : nullptr;
+    const uint16_t *pn = MODE == SW_PRECON ? A.nbits + q0 : nullptr;
+    T *pout = A.out + q0;
+    float *pout32 = A.out32 ? A.out32 + q0 : nullptr;
+    unsigned long long *xbuf = A.xch;
+    const unsigned long long *pxj = xbuf + xj0, *pxk = xbuf + xk0;
+    unsigned long long *pxo = xbuf + xo0;
 
-    // exchanged value: FWD w = (negscale*precon)*q; BWD z; PRECON precon
-    T prev = T(0);
-    double dot = 0.0;
-    for (int s = 0; s < S; s++) {
-        int i;
-        if (MODE == SW_BWD) i = (c.nx - 1) - (s - (BJ - 1 - jl) - (BK - 1 - kl));
-        else i = s - jl - kl;
-        const bool act = valid && i >= 0 && i < c.nx;
-        T xch = T(0);
-        if (act) {
-            const long long e = c.at(i, j, k);
-            const uint8_t fl = A.flags[e];
-            // neighbour values of the previous step
-            T nj_, nk_;
-            if (MODE == SW_BWD) {
-                if (jl < BJ - 1) nj_ = xb[(s - 1) & 1][kl][jl + 1];
-                else nj_ = ldcg(A.out + e + sy);
-                if (kl < BK - 1) nk_ = xb[(s - 1) & 1][kl + 1][jl];
-                else nk_ = ldcg(A.out + e + sz);
-            } else if (MODE == SW_FWD) {
-                if (jl > 0) nj_ = xb[(s - 1) & 1][kl][jl - 1];
-                else nj_ = Op::mul(Op::mul(A.negscale, A.precon[e - sy]), ldcg(A.out + e - sy));
-                if (kl > 0) nk_ = xb[(s - 1) & 1][kl - 1][jl];
-                else nk_ = Op::mul(Op::mul(A.negscale, A.precon[e - sz]), ldcg(A.out + e - sz));
-            } else {
-                if (jl > 0) nj_ = xb[(s - 1) & 1][kl][jl - 1];
-                else nj_ = ldcg(A.out + e - sy);
-                if (kl > 0) nk_ = xb[(s - 1) & 1][kl - 1][jl];
-                else nk_ = ldcg(A.out + e - sz);
-            }
-            T val = T(0);
-            if (fl & GFS_PF_FLUID) {
+    // ring slot u holds the inputs of step s0 + u (FWD/BWD: cp.async into shared
+    // memory; PRECON, once per solve: registers)
+    unsigned r_f[P], r_n[P];
+    unsigned long long r_wj[PE][X::W], r_wk[PE][X::W];
+    auto prefetch = [&](int st, int u) {
+        const bool ok = st >= st_lo && st < st_hi;
+        const long long o = (long long)st * PS;
+        if (MODE == SW_PRECON) {
+            r_f[u] = ok ? ld_nc_u8(pf + o) : 0u;
+            r_n[u] = ok ? ld_nc_u16(pn + o) : 0u;
+        } else {
+            // a zero-size source fills the slot with zeros
+            cp_async<sizeof(T)>(&ring[0][u][tid], ok ? pa + o : pa, ok);
+            cp_async<sizeof(T)>(&ring[1][u][tid], ok ? pb + o : pb, ok);
+            if (MODE == SW_BWD) cp_async<sizeof(T)>(&ring[MODE == SW_BWD ? 2 : 0][u][tid], ok ? pc_ + o : pc_, ok);
+            cp_async_commit();
+        }
+    };
+    auto prefetch_x = [&](int st, int v) {
+        const bool ok = st >= st_lo && st < st_hi;
+        if (in_j && ok) {
+            const unsigned long long *q = pxj + (long long)st * XS;
+            r_wj[v][0] = ld_cg_u64(q);
+            if (X::W == 2) r_wj[v][X::W - 1] = ld_cg_u64(q + 1);
+        }
+        if (in_k && ok) {
+            const unsigned long long *q = pxk + (long long)st * XS;
+            r_wk[v][0] = ld_cg_u64(q);
+            if (X::W == 2) r_wk[v][X::W - 1] = ld_cg_u64(q + 1);
+        }
+    };
+#pragma unroll
+    for (int u = 0; u < P; u++) prefetch(u, u);
+#pragma unroll
+    for (int v = 0; v < PE; v++) prefetch_x(v, v);
+
+    T prev = T(0);       // exchanged value of this pencil's previous cell
+    Acc2f dot32;         // BWD, FP32: compensated dot(z, r)
+    double dot64 = 0.0;  // BWD, FP64
+    static_assert(P % PE == 0, "exchange ring must divide the input ring");
+    const int SP = ((S + P - 1) / P) * P;
+    for (int s0 = 0; s0 < SP; s0 += P) {
+#pragma unroll
+        for (int u = 0; u < P; u++) {
+            const int st = s0 + u;
+            const int v = u % PE;
+            if (MODE != SW_PRECON) cp_async_wait<P - 1>();   // this step's copies have landed
+            T xch = T(0);
+            if (st >= st_lo && st < st_hi) {
+                const long long o = (long long)st * PS;
+                T nj_, nk_;
+                if (!at_j) nj_ = xb[(st - 1) & 1][kl][xj];
+                else nj_ = in_j ? xch_take<T>(r_wj[v], pxj + (long long)st * XS, tag, A.ctrl, timed_out) : T(0);
+                if (!at_k) nk_ = xb[(st - 1) & 1][xk][jl];
+                else nk_ = in_k ? xch_take<T>(r_wk[v], pxk + (long long)st * XS, tag, A.ctrl, timed_out) : T(0);
+                T val = T(0);
                 if (MODE == SW_FWD) {
-                    // _applyPreconditioner forward solve (pressuresolver.cpp:311-351)
-                    T pc = A.precon[e];
-                    T tt = Op::sub(Op::sub(Op::sub(A.in[e], prev), nj_), nk_);
+                    // _applyPreconditioner forward solve (pressuresolver.cpp:311-351); neighbours hand
+                    // over (negscale*precon)*q.  precon is 0 off the fluid set, so those cells give 0.
+                    T pc = ring[1][u][tid];
+                    T tt = Op::sub(Op::sub(Op::sub(ring[0][u][tid], prev), nj_), nk_);
                     val = Op::mul(tt, pc);
                     xch = Op::mul(Op::mul(A.negscale, pc), val);
                 } else if (MODE == SW_BWD) {
                     // backward solve (pressuresolver.cpp:354-385)
-                    T pc = A.precon[e];
+                    T pc = ring[1][u][tid];
                     T m = Op::mul(A.negscale, pc);
-                    T tt = Op::sub(Op::sub(Op::sub(A.in[e], Op::mul(m, prev)), Op::mul(m, nj_)),
+                    T tt = Op::sub(Op::sub(Op::sub(ring[0][u][tid], Op::mul(m, prev)), Op::mul(m, nj_)),
                                    Op::mul(m, nk_));
                     val = Op::mul(tt, pc);
                     xch = val;
-                    dot += (double)val * (double)A.rdot[e];
+                    const T rv = ring[MODE == SW_BWD ? 2 : 0][u][tid];
+                    if (sizeof(T) == 4) dot32.add((float)val * (float)rv);
+                    else dot64 += (double)val * (double)rv;
                 } else {
-                    val = (T)mic0_precon(A.flags, c, e, fl, (double)prev, (double)nj_, (double)nk_,
-                                         A.scale, A.dnegscale);
+                    const uint8_t fl = (uint8_t)r_f[u];
+                    if (fl & GFS_PF_FLUID) val = mic0_precon<T>(r_n[u], fl, prev, nj_, nk_, (T)A.scale, A.negscale);
                     xch = val;
-                    if (A.out32) A.out32[e] = (float)val;
                 }
-            } else if (MODE == SW_PRECON && A.out32) {
-                A.out32[e] = 0.0f;
+                pout[o] = val;
+                if (MODE == SW_PRECON && pout32) pout32[o] = (float)val;
+                if (out_j) X::put(pxo + (long long)st * XS + (long long)kl * X::W, xch, tag);
+                if (out_k) X::put(pxo + (long long)st * XS + (long long)(SBJ + jl) * X::W, xch, tag);
             }
-            A.out[e] = val;
+            xb[st & 1][kl][jl] = xch;
+            prev = xch;
+            prefetch(st + P, u);
+            prefetch_x(st + PE, v);
+            __syncthreads();
         }
-        xb[s & 1][kl][jl] = xch;
-        prev = xch;
-        if (tid == 0 && !timed_out) {
-            st_release_u32(mine, (unsigned)s);   // steps 0..s-1 are complete
-            unsigned nxt = (unsigned)min(s + 1 + BJ, S), nxk = (unsigned)min(s + 1 + BK, S);
-            if (prod_j) wait_progress(prod_j, nxt, cj, timed_out, A.ctrl);
-            if (prod_k) wait_progress(prod_k, nxk, ck, timed_out, A.ctrl);
-        }
-        __syncthreads();
     }
-    if (tid == 0) st_release_u32(mine, (unsigned)S);
+    if (MODE != SW_PRECON) cp_async_wait<0>();
 
     // block partial of dot(z, r) and the last-CTA epilogue
     double part = 0.0;
-    if (MODE == SW_BWD) part = block_reduce<0>(dot);
+    if (MODE == SW_BWD) part = block_reduce<0>(sizeof(T) == 4 ? dot32.value() : dot64);
     __shared__ bool last;
-    unsigned nblocks = (unsigned)(A.nbj * A.nbk);
+    const unsigned nblocks = (unsigned)(K.nbj * K.nbk);
     if (tid == 0) {
-        if (MODE == SW_BWD) A.partials[bj + A.nbj * bk] = part;
+        if (MODE == SW_BWD) A.partials[bj + K.nbj * bk] = part;
         __threadfence();
         unsigned tk = atomicAdd(A.done_ticket, 1u);
         last = tk == nblocks - 1;
@@ -383,10 +680,9 @@ __global__ void __launch_bounds__(BJ *BK) k_sweep(SweepArgs<T> A) {
     __syncthreads();
     if (!last) return;
     __threadfence();
-    for (unsigned q = tid; q < nblocks; q += BJ * BK) A.progress[q] = 0;
     if (MODE == SW_BWD) {
         double acc = 0.0;
-        for (unsigned q = tid; q < nblocks; q += BJ * BK) acc += __ldcg(A.partials + q);
+        for (unsigned q = tid; q < nblocks; q += SWEEP_THREADS) acc += __ldcg(A.partials + q);
         acc = block_reduce<0>(acc);
         if (tid == 0) {
             PsCtrl *C = A.ctrl;
@@ -405,6 +701,7 @@ __global__ void __launch_bounds__(BJ *BK) k_sweep(SweepArgs<T> A) {
     if (tid == 0) {
         *A.ticket = 0;
         *A.done_ticket = 0;
+        A.ctrl->epoch = tag + 1 == 0 ? 1u : tag + 1;   // the next sweep's tag (0 marks never written)
     }
 }
 
@@ -412,13 +709,30 @@ __global__ void __launch_bounds__(BJ *BK) k_sweep(SweepArgs<T> A) {
 
 template <class T>
 struct VecArgs {
-    GridDim c;
-    const uint8_t *flags;
+    Skew K;
+    const uint8_t *fsk;
     T negscale, scale;
     double *partials;
     PsCtrl *ctrl;
     int mixed;
 };
+
+// x at the six neighbours of slot q in the skewed layout, in the reference's
+// summation order i-1, i+1, j-1, j+1, k-1, k+1 (0 outside the grid).
+template <class T>
+__device__ __forceinline__ T neighbour_sum(const Skew &K, const T *__restrict__ x, long long q) {
+    using Op = Ar<T>;
+    int bj, bk, s, jl, kl;
+    K.decode(q, bj, bk, s, jl, kl);
+    const int i = s - jl - kl;
+    T xim = i > 0 ? x[q - SPLANE] : T(0);
+    T xip = i < K.nx - 1 ? x[q + SPLANE] : T(0);
+    T xjm = jl > 0 ? x[q - SPLANE - 1] : (bj > 0 ? x[K.slot(bj - 1, bk, s + SBJ - 1, SBJ - 1, kl)] : T(0));
+    T xjp = jl < SBJ - 1 ? x[q + SPLANE + 1] : (bj + 1 < K.nbj ? x[K.slot(bj + 1, bk, s - SBJ + 1, 0, kl)] : T(0));
+    T xkm = kl > 0 ? x[q - SPLANE - SBJ] : (bk > 0 ? x[K.slot(bj, bk - 1, s + SBK - 1, jl, SBK - 1)] : T(0));
+    T xkp = kl < SBK - 1 ? x[q + SPLANE + SBJ] : (bk + 1 < K.nbk ? x[K.slot(bj, bk + 1, s - SBK + 1, jl, 0)] : T(0));
+    return Op::add(Op::add(Op::add(Op::add(Op::add(xim, xip), xjm), xjp), xkm), xkp);
+}
 
 // As = A s and dot(As, s) -> alpha (pressuresolver.cpp:388-426, :472-473)
 template <class T>
@@ -426,22 +740,21 @@ __global__ void __launch_bounds__(RED_THREADS) k_matvec(VecArgs<T> A, const T *_
                                                         T *__restrict__ As) {
     using Op = Ar<T>;
     if (A.ctrl->done) return;
-    const GridDim &c = A.c;
-    const long long sy = c.sx, sz = (long long)c.sx * c.sy;
-    double dot = 0.0;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < c.size;
-         e += (long long)gridDim.x * blockDim.x) {
-        uint8_t fl = A.flags[e];
+    const Skew &K = A.K;
+    double dot = 0.0;   // FP64 operands
+    Acc2f dot32;        // FP32 operands: compensated
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < K.size;
+         q += (long long)gridDim.x * blockDim.x) {
+        uint8_t fl = A.fsk[q];
         if (!(fl & GFS_PF_FLUID)) continue;
-        T x = s[e];
-        T val = Op::add(Op::add(Op::add(Op::add(Op::add(s[e - 1], s[e + 1]), s[e - sy]), s[e + sy]), s[e - sz]),
-                        s[e + sz]);
-        val = Op::mul(val, A.negscale);
+        T x = s[q];
+        T val = Op::mul(neighbour_sum<T>(K, s, q), A.negscale);
         val = Op::add(val, Op::mul(Op::mul((T)(fl >> 1), A.scale), x));
-        As[e] = val;
-        dot += (double)val * (double)x;
+        As[q] = val;
+        if (sizeof(T) == 4) dot32.add((float)val * (float)x);
+        else dot += (double)val * (double)x;
     }
-    double part = block_reduce<0>(dot);
+    double part = block_reduce<0>(sizeof(T) == 4 ? dot32.value() : dot);
     double res;
     if (finish_reduce<0>(part, A.partials, &A.ctrl->tickets[1], gridDim.x, &res) && threadIdx.x == 0)
         A.ctrl->alpha = A.ctrl->sigma / res;
@@ -454,18 +767,17 @@ __global__ void __launch_bounds__(RED_THREADS) k_axpy(VecArgs<T> A, T *__restric
     using Op = Ar<T>;
     PsCtrl *C = A.ctrl;
     if (C->done) return;
-    const GridDim &c = A.c;
     const T alpha = (T)C->alpha, nalpha = (T)(-C->alpha);
-    double mx = 0.0;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < c.size;
-         e += (long long)gridDim.x * blockDim.x) {
-        if (!(A.flags[e] & GFS_PF_FLUID)) continue;
-        p[e] = Op::add(p[e], Op::mul(s[e], alpha));
-        T rv = Op::add(r[e], Op::mul(As[e], nalpha));
-        r[e] = rv;
-        mx = fmax(mx, fabs((double)rv));
+    T mx = T(0);
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < A.K.size;
+         q += (long long)gridDim.x * blockDim.x) {
+        if (!(A.fsk[q] & GFS_PF_FLUID)) continue;
+        p[q] = Op::add(p[q], Op::mul(s[q], alpha));
+        T rv = Op::add(r[q], Op::mul(As[q], nalpha));
+        r[q] = rv;
+        mx = fmax(mx, fabs(rv));
     }
-    double part = block_reduce<1>(mx);
+    double part = block_reduce<1>((double)mx);
     double res;
     if (finish_reduce<1>(part, A.partials, &C->tickets[2], gridDim.x, &res) && threadIdx.x == 0) {
         C->maxr = res;
@@ -483,27 +795,25 @@ __global__ void __launch_bounds__(RED_THREADS) k_update_s(VecArgs<T> A, const T 
                                                           T *__restrict__ s) {
     using Op = Ar<T>;
     if (A.ctrl->done) return;
-    const GridDim &c = A.c;
     const T beta = (T)A.ctrl->beta;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < c.size;
-         e += (long long)gridDim.x * blockDim.x) {
-        if (!(A.flags[e] & GFS_PF_FLUID)) continue;
-        s[e] = Op::add(Op::mul(z[e], (T)1.0), Op::mul(s[e], beta));
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < A.K.size;
+         q += (long long)gridDim.x * blockDim.x) {
+        if (!(A.fsk[q] & GFS_PF_FLUID)) continue;
+        s[q] = Op::add(Op::mul(z[q], (T)1.0), Op::mul(s[q], beta));
     }
 }
 
 // MIXED: r32 = (float) r64, e32 = 0, s32 = 0; inner threshold from max|r64|.
-__global__ void __launch_bounds__(RED_THREADS) k_mixed_prepare(GridDim c, const uint8_t *__restrict__ flags,
+__global__ void __launch_bounds__(RED_THREADS) k_mixed_prepare(Skew K, const uint8_t *__restrict__ fsk,
                                                                const double *__restrict__ r64,
                                                                float *__restrict__ r32, float *__restrict__ e32,
-                                                               float *__restrict__ s32, PsCtrl *ctrl,
-                                                               double eta) {
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < c.size;
-         e += (long long)gridDim.x * blockDim.x) {
-        bool f = flags[e] & GFS_PF_FLUID;
-        r32[e] = f ? (float)r64[e] : 0.0f;
-        e32[e] = 0.0f;
-        s32[e] = 0.0f;
+                                                               float *__restrict__ s32, PsCtrl *ctrl, double eta) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < K.size;
+         q += (long long)gridDim.x * blockDim.x) {
+        bool f = fsk[q] & GFS_PF_FLUID;
+        r32[q] = f ? (float)r64[q] : 0.0f;
+        e32[q] = 0.0f;
+        s32[q] = 0.0f;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         double m = ctrl->maxr64;
@@ -516,30 +826,30 @@ __global__ void __launch_bounds__(RED_THREADS) k_mixed_prepare(GridDim c, const 
     }
 }
 
-// MIXED: p64 += e32, then r64 = b - A p64 in FP64 and max|r64| (outer refinement).
-__global__ void __launch_bounds__(RED_THREADS) k_mixed_correct(GridDim c, const uint8_t *__restrict__ flags,
+// MIXED: p64 += e32 (outer refinement)
+__global__ void __launch_bounds__(RED_THREADS) k_mixed_correct(Skew K, const uint8_t *__restrict__ fsk,
                                                                double *__restrict__ p64,
                                                                const float *__restrict__ e32) {
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < c.size;
-         e += (long long)gridDim.x * blockDim.x)
-        if (flags[e] & GFS_PF_FLUID) p64[e] += (double)e32[e];
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < K.size;
+         q += (long long)gridDim.x * blockDim.x)
+        if (fsk[q] & GFS_PF_FLUID) p64[q] += (double)e32[q];
 }
 
+// MIXED: r64 = b - A p64 in FP64 and max|r64|
 __global__ void __launch_bounds__(RED_THREADS) k_residual64(VecArgs<double> A, const double *__restrict__ b,
                                                             const double *__restrict__ p,
                                                             double *__restrict__ r) {
     using Op = Ar<double>;
-    const GridDim &c = A.c;
-    const long long sy = c.sx, sz = (long long)c.sx * c.sy;
+    const Skew &K = A.K;
     double mx = 0.0;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < c.size;
-         e += (long long)gridDim.x * blockDim.x) {
-        uint8_t fl = A.flags[e];
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < K.size;
+         q += (long long)gridDim.x * blockDim.x) {
+        uint8_t fl = A.fsk[q];
         if (!(fl & GFS_PF_FLUID)) continue;
-        double val = p[e - 1] + p[e + 1] + p[e - sy] + p[e + sy] + p[e - sz] + p[e + sz];
-        val = Op::add(Op::mul(val, A.negscale), Op::mul(Op::mul((double)(fl >> 1), A.scale), p[e]));
-        double rv = b[e] - val;
-        r[e] = rv;
+        double val = Op::mul(neighbour_sum<double>(K, p, q), A.negscale);
+        val = Op::add(val, Op::mul(Op::mul((double)(fl >> 1), A.scale), p[q]));
+        double rv = b[q] - val;
+        r[q] = rv;
         mx = fmax(mx, fabs(rv));
     }
     double part = block_reduce<1>(mx);
@@ -553,35 +863,47 @@ __global__ void __launch_bounds__(RED_THREADS) k_residual64(VecArgs<double> A, c
 
 // --------------------------------------------------------------- driver
 
-static constexpr int BJ64 = 8, BK64 = 8;     // FP64 sweeps: FP64 issue rate favours small CTAs
-static constexpr int BJ32 = 16, BK32 = 16;   // FP32 sweeps
-
 static int ensure_ws(Ctx *ctx, PressureWs &ws, const Grids &g, bool mixed) {
     long long n = g.c.size;
+    Skew K = make_skew(g.c);
     if (ws.allocated_for != n) {
         ws.c = g.c;
+        ws.nbj = K.nbj;
+        ws.nbk = K.nbk;
+        ws.skew_size = K.size;
         int rc = 0;
         rc |= ws.flags.alloc((size_t)n);
-        DevMem *v64[] = {&ws.b, &ws.p, &ws.r, &ws.z, &ws.s, &ws.As, &ws.q, &ws.precon};
-        for (DevMem *m : v64) rc |= m->alloc((size_t)n * sizeof(double));
+        rc |= ws.b.alloc((size_t)n * sizeof(double));
+        rc |= ws.p.alloc((size_t)n * sizeof(double));
+        rc |= ws.fsk.alloc((size_t)K.size);
+        DevMem *v64[] = {&ws.bsk, &ws.psk, &ws.r, &ws.z, &ws.s, &ws.As, &ws.q, &ws.precon};
+        for (DevMem *m : v64) rc |= m->alloc((size_t)K.size * sizeof(double));
         if (rc) return GFS_ERR_NOMEM;
         for (DevMem *m : v64) GFS_CUDA_CHECK(cudaMemsetAsync(m->p, 0, m->bytes, ctx->stream));
         GFS_CUDA_CHECK(cudaMemsetAsync(ws.flags.p, 0, ws.flags.bytes, ctx->stream));
+        GFS_CUDA_CHECK(cudaMemsetAsync(ws.fsk.p, 0, ws.fsk.bytes, ctx->stream));
+        GFS_CUDA_CHECK(cudaMemsetAsync(ws.b.p, 0, ws.b.bytes, ctx->stream));
+        GFS_CUDA_CHECK(cudaMemsetAsync(ws.p.p, 0, ws.p.bytes, ctx->stream));
         ws.nblocks_red = (size_t)ctx->num_sms * 8;
-        int nbmax = (int)(((g.c.ny + 7) / 8) * ((g.c.nz + 7) / 8));
-        size_t np = ws.nblocks_red > (size_t)nbmax ? ws.nblocks_red : (size_t)nbmax;
+        size_t nbl = (size_t)K.nbj * K.nbk;
+        size_t np = ws.nblocks_red > nbl ? ws.nblocks_red : nbl;
         if (ws.partials.alloc(np * sizeof(double))) return GFS_ERR_NOMEM;
         if (ws.ctrl.alloc(sizeof(PsCtrl))) return GFS_ERR_NOMEM;
         GFS_CUDA_CHECK(cudaMemsetAsync(ws.ctrl.p, 0, sizeof(PsCtrl), ctx->stream));
-        if (ws.progress.alloc((size_t)nbmax * sizeof(unsigned))) return GFS_ERR_NOMEM;
-        GFS_CUDA_CHECK(cudaMemsetAsync(ws.progress.p, 0, ws.progress.bytes, ctx->stream));
+        // exchange words: per block and plane XCH_PER_PLANE entries of up to 2 words
+        size_t nx_words = nbl * (size_t)K.S * XCH_PER_PLANE * 2;
+        if (ws.xch.alloc(nx_words * sizeof(unsigned long long))) return GFS_ERR_NOMEM;
+        GFS_CUDA_CHECK(cudaMemsetAsync(ws.xch.p, 0, ws.xch.bytes, ctx->stream));
+        if (ws.nbstd.alloc((size_t)n * sizeof(uint16_t)) || ws.nbsk.alloc((size_t)K.size * sizeof(uint16_t)))
+            return GFS_ERR_NOMEM;
+        GFS_CUDA_CHECK(cudaMemsetAsync(ws.nbsk.p, 0, ws.nbsk.bytes, ctx->stream));
         ws.allocated_for = n;
         ws.mixed_alloc = false;
     }
     if (mixed && !ws.mixed_alloc) {
         DevMem *v32[] = {&ws.r32, &ws.z32, &ws.s32, &ws.As32, &ws.q32, &ws.e32, &ws.precon32};
         for (DevMem *m : v32) {
-            if (m->alloc((size_t)n * sizeof(float))) return GFS_ERR_NOMEM;
+            if (m->alloc((size_t)K.size * sizeof(float))) return GFS_ERR_NOMEM;
             GFS_CUDA_CHECK(cudaMemsetAsync(m->p, 0, m->bytes, ctx->stream));
         }
         ws.mixed_alloc = true;
@@ -589,15 +911,14 @@ static int ensure_ws(Ctx *ctx, PressureWs &ws, const Grids &g, bool mixed) {
     return GFS_OK;
 }
 
-template <class T, int BJ, int BK, int MODE>
+template <class T, int MODE, int P = (sizeof(T) == 8 ? 4 : 8), int PE = 2>
 static int launch_sweep(Ctx *ctx, PressureWs &ws, const T *in, T *out, const T *precon, const T *rdot,
                         float *out32, double scale, int init) {
     SweepArgs<T> A;
+    A.K = make_skew(ws.c);
     A.c = ws.c;
-    A.nbj = (ws.c.ny + BJ - 1) / BJ;
-    A.nbk = (ws.c.nz + BK - 1) / BK;
-    A.S = ws.c.nx + BJ + BK - 2;
-    A.flags = ws.flags.as<uint8_t>();
+    A.fsk = ws.fsk.as<uint8_t>();
+    A.fstd = ws.flags.as<uint8_t>();
     A.in = in;
     A.out = out;
     A.precon = precon;
@@ -606,14 +927,16 @@ static int launch_sweep(Ctx *ctx, PressureWs &ws, const T *in, T *out, const T *
     A.negscale = (T)(-scale);
     A.scale = scale;
     A.dnegscale = -scale;
-    A.progress = ws.progress.as<unsigned>();
+    A.xch = ws.xch.as<unsigned long long>();
+    A.nbits = ws.nbsk.as<uint16_t>();
     PsCtrl *C = ws.ctrl.as<PsCtrl>();
     A.ticket = &C->sweep_ticket[MODE];
     A.done_ticket = &C->tickets[0];
     A.partials = ws.partials.as<double>();
     A.ctrl = C;
     A.init = init;
-    k_sweep<T, BJ, BK, MODE><<<A.nbj * A.nbk, BJ * BK, 0, ctx->stream>>>(A);
+    ProfScope prof(ctx, MODE == SW_FWD ? KC_SWEEP_FWD : (MODE == SW_BWD ? KC_SWEEP_BWD : KC_PRECON));
+    k_sweep<T, MODE, P, PE><<<A.K.nbj * A.K.nbk, SWEEP_THREADS, 0, ctx->stream>>>(A);
     ctx->launches++;
     GFS_LAUNCH_CHECK();
     return GFS_OK;
@@ -622,8 +945,8 @@ static int launch_sweep(Ctx *ctx, PressureWs &ws, const T *in, T *out, const T *
 template <class T>
 static VecArgs<T> vec_args(PressureWs &ws, double scale, int mixed) {
     VecArgs<T> A;
-    A.c = ws.c;
-    A.flags = ws.flags.as<uint8_t>();
+    A.K = make_skew(ws.c);
+    A.fsk = ws.fsk.as<uint8_t>();
     A.negscale = (T)(-scale);
     A.scale = (T)scale;
     A.partials = ws.partials.as<double>();
@@ -633,18 +956,25 @@ static VecArgs<T> vec_args(PressureWs &ws, double scale, int mixed) {
 }
 
 // One CG iteration (matvec, update, forward + backward MIC(0) solve, new search direction).
-template <class T, int BJ, int BK>
+template <class T>
 static int cg_iteration(Ctx *ctx, PressureWs &ws, double scale, int mixed, T *p, T *r, T *z, T *s, T *As,
                         T *q, const T *precon) {
     unsigned nb = (unsigned)ws.nblocks_red;
     VecArgs<T> V = vec_args<T>(ws, scale, mixed);
-    k_matvec<T><<<nb, RED_THREADS, 0, ctx->stream>>>(V, s, As);
-    k_axpy<T><<<nb, RED_THREADS, 0, ctx->stream>>>(V, p, r, s, As);
+    {
+        ProfScope prof(ctx, KC_MATVEC);
+        k_matvec<T><<<nb, RED_THREADS, 0, ctx->stream>>>(V, s, As);
+    }
+    {
+        ProfScope prof(ctx, KC_AXPY);
+        k_axpy<T><<<nb, RED_THREADS, 0, ctx->stream>>>(V, p, r, s, As);
+    }
     ctx->launches += 2;
-    int rc = launch_sweep<T, BJ, BK, SW_FWD>(ctx, ws, r, q, precon, nullptr, nullptr, scale, 0);
+    int rc = launch_sweep<T, SW_FWD>(ctx, ws, r, q, precon, nullptr, nullptr, scale, 0);
     if (rc) return rc;
-    rc = launch_sweep<T, BJ, BK, SW_BWD>(ctx, ws, q, z, precon, r, nullptr, scale, 0);
+    rc = launch_sweep<T, SW_BWD>(ctx, ws, q, z, precon, r, nullptr, scale, 0);
     if (rc) return rc;
+    ProfScope prof(ctx, KC_UPDATE_S);
     k_update_s<T><<<nb, RED_THREADS, 0, ctx->stream>>>(V, z, s);
     ctx->launches++;
     GFS_LAUNCH_CHECK();
@@ -673,6 +1003,7 @@ int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
     const double dx = g.dx;
     const double scale = dt / (density * dx * dx);   // pressuresolver.cpp:250
     PsCtrl *C = ws.ctrl.as<PsCtrl>();
+    const Skew K = make_skew(g.c);
     // tolerance / cap into the control block
     {
         PsCtrl h;
@@ -682,6 +1013,7 @@ int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
         h.tol = tol;
         h.max_iters = max_iters;
         h.err = 0;
+        if (h.epoch == 0) h.epoch = 1;   // exchange words start zeroed: tag 0 means "never written"
         GFS_CUDA_CHECK(cudaMemcpyAsync(C, &h, sizeof(PsCtrl), cudaMemcpyHostToDevice, st));
     }
     SetupArgs SA;
@@ -693,10 +1025,17 @@ int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
     SA.scale_div = (double)(1.0f / (float)dx);
     SA.tol = tol;
     unsigned nb = (unsigned)ws.nblocks_red;
-    k_ps_setup<<<nb, RED_THREADS, 0, st>>>(SA, mat, mac[0], mac[1], mac[2], ws.flags.as<uint8_t>(),
-                                            ws.b.as<double>(), ws.r.as<double>(), ws.p.as<double>(),
-                                            ws.s.as<double>(), ws.partials.as<double>(), C);
-    ctx->launches++;
+    {
+        ProfScope prof(ctx, KC_PS_SETUP);
+        k_ps_setup<<<nb, RED_THREADS, 0, st>>>(SA, mat, mac[0], mac[1], mac[2], ws.flags.as<uint8_t>(),
+                                                ws.b.as<double>(), ws.partials.as<double>(), C);
+        dim3 cgrid(grid_blocks(g.c.nx, 128), g.c.ny, g.c.nz);
+        k_nbits<<<cgrid, 128, 0, st>>>(g.c, ws.flags.as<uint8_t>(), ws.nbstd.as<uint16_t>());
+        k_to_skew<<<nb, RED_THREADS, 0, st>>>(K, g.c, ws.flags.as<uint8_t>(), ws.b.as<double>(),
+                                               ws.nbstd.as<uint16_t>(), ws.fsk.as<uint8_t>(), ws.nbsk.as<uint16_t>(), ws.bsk.as<double>(), ws.r.as<double>(),
+                                               ws.psk.as<double>(), ws.s.as<double>());
+    }
+    ctx->launches += 3;
     GFS_LAUNCH_CHECK();
     PsCtrl h;
     rc = read_ctrl(ctx, ws, &h);
@@ -704,26 +1043,31 @@ int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
     int iterations = h.iter;
     double final_res = h.maxb;
     int refinements = 0;
+    int sweeps = 0;   // forward (= backward) MIC(0) solves that did work
     if (!h.done) {
         // MIC(0) preconditioner (pressuresolver.cpp:246-302), FP64 in both modes
-        rc = launch_sweep<double, BJ64, BK64, SW_PRECON>(ctx, ws, nullptr, ws.precon.as<double>(), nullptr,
-                                                         nullptr, mixed ? ws.precon32.as<float>() : nullptr,
-                                                         scale, 0);
+        if (mixed) rc = launch_sweep<float, SW_PRECON>(ctx, ws, nullptr, ws.precon32.as<float>(), nullptr, nullptr,
+                                                       nullptr, scale, 0);
+        else rc = launch_sweep<double, SW_PRECON>(ctx, ws, nullptr, ws.precon.as<double>(), nullptr, nullptr, nullptr,
+                                                  scale, 0);
         if (rc) return rc;
         if (!mixed) {
-            double *p = ws.p.as<double>(), *r = ws.r.as<double>(), *z = ws.z.as<double>(),
+            double *p = ws.psk.as<double>(), *r = ws.r.as<double>(), *z = ws.z.as<double>(),
                    *s = ws.s.as<double>(), *As = ws.As.as<double>(), *q = ws.q.as<double>(),
                    *pc = ws.precon.as<double>();
-            rc = launch_sweep<double, BJ64, BK64, SW_FWD>(ctx, ws, r, q, pc, nullptr, nullptr, scale, 0);
+            rc = launch_sweep<double, SW_FWD>(ctx, ws, r, q, pc, nullptr, nullptr, scale, 0);
             if (rc) return rc;
-            rc = launch_sweep<double, BJ64, BK64, SW_BWD>(ctx, ws, q, z, pc, r, nullptr, scale, 1);
+            rc = launch_sweep<double, SW_BWD>(ctx, ws, q, z, pc, r, nullptr, scale, 1);
             if (rc) return rc;
             VecArgs<double> V = vec_args<double>(ws, scale, 0);
-            k_update_s<double><<<nb, RED_THREADS, 0, st>>>(V, z, s);
+            {
+                ProfScope prof(ctx, KC_UPDATE_S);
+                k_update_s<double><<<nb, RED_THREADS, 0, st>>>(V, z, s);
+            }
             ctx->launches++;
             for (;;) {
                 for (int it = 0; it < CG_CHUNK; it++) {
-                    rc = cg_iteration<double, BJ64, BK64>(ctx, ws, scale, 0, p, r, z, s, As, q, pc);
+                    rc = cg_iteration<double>(ctx, ws, scale, 0, p, r, z, s, As, q, pc);
                     if (rc) return rc;
                 }
                 rc = read_ctrl(ctx, ws, &h);
@@ -732,6 +1076,7 @@ int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
             }
             iterations = h.iter;
             final_res = h.maxr;
+            sweeps = 1 + h.iter;
         } else {
             const double eta = 1e-3;
             float *r32 = ws.r32.as<float>(), *z32 = ws.z32.as<float>(), *s32 = ws.s32.as<float>(),
@@ -743,24 +1088,29 @@ int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
             VecArgs<double> V64 = vec_args<double>(ws, scale, 1);
             VecArgs<float> V32 = vec_args<float>(ws, scale, 1);
             while (total < max_iters) {
-                k_mixed_prepare<<<nb, RED_THREADS, 0, st>>>(g.c, ws.flags.as<uint8_t>(), ws.r.as<double>(), r32,
-                                                           e32, s32, C, eta);
+                {
+                    ProfScope prof(ctx, KC_MIXED_AUX);
+                    k_mixed_prepare<<<nb, RED_THREADS, 0, st>>>(K, ws.fsk.as<uint8_t>(), ws.r.as<double>(), r32,
+                                                               e32, s32, C, eta);
+                }
                 ctx->launches++;
                 // the inner cap is what is left of the total budget
                 {
                     int left = max_iters - total;
                     GFS_CUDA_CHECK(cudaMemcpyAsync(&C->max_iters, &left, sizeof(int), cudaMemcpyHostToDevice, st));
                 }
-                rc = launch_sweep<float, BJ32, BK32, SW_FWD>(ctx, ws, r32, q32, pc32, nullptr, nullptr, scale, 0);
+                rc = launch_sweep<float, SW_FWD>(ctx, ws, r32, q32, pc32, nullptr, nullptr, scale, 0);
                 if (rc) return rc;
-                rc = launch_sweep<float, BJ32, BK32, SW_BWD>(ctx, ws, q32, z32, pc32, r32, nullptr, scale, 1);
+                rc = launch_sweep<float, SW_BWD>(ctx, ws, q32, z32, pc32, r32, nullptr, scale, 1);
                 if (rc) return rc;
-                k_update_s<float><<<nb, RED_THREADS, 0, st>>>(V32, z32, s32);
+                {
+                    ProfScope prof(ctx, KC_UPDATE_S);
+                    k_update_s<float><<<nb, RED_THREADS, 0, st>>>(V32, z32, s32);
+                }
                 ctx->launches++;
                 for (;;) {
                     for (int it = 0; it < CG_CHUNK; it++) {
-                        rc = cg_iteration<float, BJ32, BK32>(ctx, ws, scale, 1, e32, r32, z32, s32, As32, q32,
-                                                             pc32);
+                        rc = cg_iteration<float>(ctx, ws, scale, 1, e32, r32, z32, s32, As32, q32, pc32);
                         if (rc) return rc;
                     }
                     rc = read_ctrl(ctx, ws, &h);
@@ -770,9 +1120,13 @@ int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
                 // h.iter counts the inner iterations that completed without converging;
                 // the converging iteration is one more.
                 total += h.converged ? h.iter + 1 : h.iter;
-                k_mixed_correct<<<nb, RED_THREADS, 0, st>>>(g.c, ws.flags.as<uint8_t>(), ws.p.as<double>(), e32);
-                k_residual64<<<nb, RED_THREADS, 0, st>>>(V64, ws.b.as<double>(), ws.p.as<double>(),
-                                                          ws.r.as<double>());
+                sweeps += 1 + h.iter;
+                {
+                    ProfScope prof(ctx, KC_MIXED_AUX);
+                    k_mixed_correct<<<nb, RED_THREADS, 0, st>>>(K, ws.fsk.as<uint8_t>(), ws.psk.as<double>(), e32);
+                    k_residual64<<<nb, RED_THREADS, 0, st>>>(V64, ws.bsk.as<double>(), ws.psk.as<double>(),
+                                                              ws.r.as<double>());
+                }
                 ctx->launches += 2;
                 rc = read_ctrl(ctx, ws, &h);
                 if (rc) return rc;
@@ -793,10 +1147,18 @@ int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
             GFS_CUDA_CHECK(cudaMemcpyAsync(&C->done, &one, sizeof(int), cudaMemcpyHostToDevice, st));
         }
     }
+    // solution back to the padded cell layout
+    {
+        dim3 grid(grid_blocks(g.c.nx, 128), g.c.ny, g.c.nz);
+        k_from_skew<<<grid, 128, 0, st>>>(K, g.c, ws.flags.as<uint8_t>(), ws.psk.as<double>(), ws.p.as<double>());
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+    }
     if (stats) {
         stats->cg_iterations = iterations;
         stats->cg_max_residual = final_res;
         stats->refinements = refinements;
+        stats->sweeps = sweeps;
     }
     return GFS_OK;
 }
@@ -844,6 +1206,7 @@ __global__ void __launch_bounds__(128) k_apply_pressure(ApplyArgs A, const uint8
 
 int pressure_apply(Sim *s, double dt) {
     Ctx *ctx = s->ctx;
+    ProfScope prof(ctx, KC_APPLY);
     ApplyArgs A;
     A.c = s->g.c;
     for (int d = 0; d < 3; d++) A.f[d] = s->g.f[d];

@@ -138,6 +138,7 @@ static float float_floor_of(double x) {
 
 int splat_velocity(Sim *s) {
     Ctx *ctx = s->ctx;
+    ProfScope prof(ctx, KC_SPLAT);
     SplatArgs A;
     A.c = s->g.c;
     for (int d = 0; d < 3; d++) A.f[d] = s->g.f[d];
@@ -223,6 +224,7 @@ __global__ void __launch_bounds__(128) k_face_fill(FillArgs A, const uint8_t *__
 
 int face_fill(Sim *s, double dt) {
     Ctx *ctx = s->ctx;
+    ProfScope prof(ctx, KC_FILL);
     FillArgs A;
     A.c = s->g.c;
     for (int d = 0; d < 3; d++) {

@@ -153,6 +153,7 @@ typedef struct gfs_step_stats {
     int64_t num_fluid_cells;
     int cg_iterations;       /* as gfs_pressure_solve                                   */
     int refinements;         /* MIXED: outer FP64 refinement steps                      */
+    int sweeps;              /* forward (= backward) MIC(0) solves that did work        */
     double cg_max_residual;  /* FP64 max|b - A p| at exit                               */
     double pressure_ms;      /* device time of the pressure solve                       */
     double step_ms;          /* device time of the whole substep                        */
@@ -209,6 +210,17 @@ int gfs_sim_step_host(gfs_sim *sim, double dt, float *h_positions, float *h_velo
 /* Number of kernel launches the library has issued on this context (for
    accounting in benchmarks). */
 int gfs_ctx_launch_count(gfs_ctx *ctx, int64_t *count);
+
+/* Optional per-kernel-class timing with CUDA events recorded on the context's
+   stream around every launch (the reference logs stage times with StopWatch,
+   fluidsimulation.cpp:3273-3389).  Classes are numbered 0..GFS_NUM_KERNEL_CLASSES-1;
+   gfs_ctx_profile_read returns a class's name, accumulated device time and
+   launch count (it synchronises the stream). */
+#define GFS_NUM_KERNEL_CLASSES 16
+int gfs_ctx_profile_enable(gfs_ctx *ctx, int on);
+int gfs_ctx_profile_reset(gfs_ctx *ctx);
+int gfs_ctx_profile_read(gfs_ctx *ctx, int index, const char **name, double *total_ms,
+                         int64_t *count);
 
 #ifdef __cplusplus
 }
