@@ -71,6 +71,7 @@ _SIGNATURES = {
     "gfs_velocity_scalar_field": [_P, _I, _I, _I, _I, _D, _P, _P, _I64, _P, _P],
     "gfs_tricubic_interpolate": [_P, _I, _I, _I, _D, _P, _P, _P, _P, _I64, _P],
     "gfs_advect_particles": [_P, _I, _I, _I, _I, _D, _P, _P, _P, _D, _P, _I64, _P],
+    "gfs_tricubic_interpolate_noalloc": [_I, _I, _I, _D, _P, _P, _P, _P, _I64, _P, _P],
     "gfs_pressure_solve": [_P, _I, _I, _I, _D, _D, _D, _P, _P, _P, _P, _I, _D, _I, _P,
                            ctypes.POINTER(_I64), ctypes.POINTER(_I), ctypes.POINTER(_D)],
     "gfs_sim_default_params": [ctypes.POINTER(SimParams)],

@@ -13,6 +13,8 @@
 // grids through the read-only path with no bounds checks (the zero halo is the
 // reference's out-of-range value).  With a power-of-two dx the stencil index
 // and the fractional offsets are formed exactly as the reference's doubles.
+#include <mutex>
+
 #include "gfs_internal.h"
 
 namespace gfs {
@@ -323,4 +325,91 @@ int interpolate_points(Ctx *ctx, const Grids &g, float *const mac[3], const floa
     return GFS_OK;
 }
 
+
+// ------------------------------------------------ no-allocation variant
+//
+// gfs_tricubic_interpolate_noalloc: the tricubic sampler of
+// gfs_tricubic_interpolate for callers that cannot allocate device memory
+// (hosts whose device memory all comes from their own allocator or arena,
+// real-time or callback code where cudaMalloc / cudaFree are not allowed).
+// The caller passes device-accessible inputs and outputs and a stream; the
+// padded copies of U, V and W that the sampler reads live in the fixed scratch
+// array below, which every GPU that loads this library keeps until the process
+// exits.  All calls share that array: two calls that overlap on the GPU race on
+// it, and each call first clears the part it uses (the halo must read as zero).
+
+#define GFS_NOALLOC_SCRATCH_FLOATS (12u << 20)   // 48 MiB: padded U+V+W of up to ~150^3 cells
+
+static __device__ __align__(256) float g_noalloc_scratch[GFS_NOALLOC_SCRATCH_FLOATS];
+
+namespace {
+std::mutex g_noalloc_mu;
+float *g_noalloc_base[256] = {nullptr};   // device address of the scratch, per device
+
+__global__ void k_pad_face(const float *__restrict__ src, GridDim g, float *__restrict__ dst) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y, k = blockIdx.z;
+    if (i >= g.nx) return;
+    dst[g.at(i, j, k)] = src[i + (long long)g.nx * (j + (long long)g.ny * k)];
+}
+}  // namespace
+
 }  // namespace gfs
+
+extern "C" int gfs_tricubic_interpolate_noalloc(int ni, int nj, int nk, double dx, const float *d_u,
+                                                const float *d_v, const float *d_w, const float *d_points,
+                                                int64_t n, float *d_out, void *stream) {
+    using namespace gfs;
+    if (ni <= 0 || nj <= 0 || nk <= 0 || !(dx > 0.0) || n < 0 || !d_u || !d_v || !d_w ||
+        (n > 0 && (!d_points || !d_out))) {
+        set_error(GFS_ERR_INVALID, "gfs_tricubic_interpolate_noalloc: invalid arguments");
+        return GFS_ERR_INVALID;
+    }
+    Grids g = make_grids(ni, nj, nk, dx);
+    unsigned long long need = (unsigned long long)g.f[0].size + g.f[1].size + g.f[2].size;
+    if (need > GFS_NOALLOC_SCRATCH_FLOATS) {
+        set_error(GFS_ERR_INVALID,
+                  "gfs_tricubic_interpolate_noalloc: a %d x %d x %d grid needs %llu scratch floats, the fixed "
+                  "scratch holds %u",
+                  ni, nj, nk, need, (unsigned)GFS_NOALLOC_SCRATCH_FLOATS);
+        return GFS_ERR_INVALID;
+    }
+    int dev = 0;
+    GFS_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) {
+        set_error(GFS_ERR_INVALID, "gfs_tricubic_interpolate_noalloc: device %d out of range", dev);
+        return GFS_ERR_INVALID;
+    }
+    float *base = nullptr;
+    {
+        // first call on this device (the current one): look up the scratch's device address
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_base[dev]) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) {
+                set_error(GFS_ERR_CUDA, "gfs_tricubic_interpolate_noalloc: cudaGetSymbolAddress: %s",
+                          cudaGetErrorString(e));
+                return GFS_ERR_CUDA;
+            }
+            g_noalloc_base[dev] = static_cast<float *>(p);
+        }
+        base = g_noalloc_base[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    float *pad[3] = {base, base + g.f[0].size, base + g.f[0].size + g.f[1].size};
+    const float *src[3] = {d_u, d_v, d_w};
+    GFS_CUDA_CHECK(cudaMemsetAsync(base, 0, (size_t)need * sizeof(float), st));
+    for (int d = 0; d < 3; d++) {
+        dim3 grid(grid_blocks(g.f[d].nx, 128), g.f[d].ny, g.f[d].nz);
+        k_pad_face<<<grid, 128, 0, st>>>(src[d], g.f[d], pad[d]);
+    }
+    GFS_LAUNCH_CHECK();
+    if (n > 0) {
+        AdvArgs A = make_adv(g, 0.0, 0.0);
+        k_points<<<grid_blocks(n, 128), 128, 0, st>>>(A, d_points, n, pad[0], pad[1], pad[2], d_out, 0, 1, 0.f, 0.f,
+                                                      0.f, 0.f);
+        GFS_LAUNCH_CHECK();
+    }
+    return GFS_OK;
+}

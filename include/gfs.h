@@ -117,6 +117,24 @@ int gfs_advect_particles(gfs_ctx *ctx, int order, int ni, int nj, int nk, double
                          const float *h_u, const float *h_v, const float *h_w, double dt,
                          const float *h_points, int64_t n, float *h_out);
 
+/* No counterpart in the reference: the tricubic sampler of gfs_tricubic_interpolate
+   for callers that cannot allocate device memory -- hosts whose device memory all
+   comes from their own allocator or arena, and real-time or callback code where
+   cudaMalloc / cudaFree are not allowed.  It allocates nothing: d_u, d_v, d_w
+   (face grids as in gfs_tricubic_interpolate), d_points (n xyz) and d_out (n xyz)
+   are device-accessible memory the caller owns, and the kernels run on the
+   caller's `stream` (a cudaStream_t; NULL = the legacy default stream).  The
+   padded copies of U, V, W it needs live in a fixed 48 MiB scratch array that
+   every GPU loading libgfs holds until the process exits; grids whose padded
+   faces need more than 12,582,912 floats (about 150^3 cells) are rejected with
+   GFS_ERR_INVALID.  The first call on a device (the current device) looks up the
+   scratch's device address; make that first call before any stream capture.
+   All calls share the scratch: calls that overlap on the GPU race on it.  The
+   call is asynchronous; results are ready when `stream` has been synchronised. */
+int gfs_tricubic_interpolate_noalloc(int ni, int nj, int nk, double dx, const float *d_u,
+                                     const float *d_v, const float *d_w, const float *d_points,
+                                     int64_t n, float *d_out, void *stream);
+
 /* -------------------------------------- pressure (PressureSolver drop-in) */
 
 /* MICCG(0) pressure solve.  Replaces PressureSolver::solve(params, pressure)
