@@ -129,6 +129,22 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def reduce_max(x: float, world: int, device: str = "cuda") -> float:
+    """Max of x over the ranks (the slowest replica sets the job time)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(steps: int, local_seconds: float, world: int, device: str = "cuda") -> float:
+    """Whole-job substeps/s of `world` independent replicas of `steps` substeps."""
+    return world * steps / reduce_max(local_seconds, world, device)
+
+
 def make_scene():
     from gridfluidsim3d_gb300 import scenes
     return scenes.slab_spheres(**SCENE)
@@ -311,10 +327,8 @@ def main(args):
             t, stats, launches = timed(ctx, sim, sc, args.steps, dt, barrier)
         _lib.lib().gfs_ctx_profile_enable(ctx.handle, 0)
         prof = profile_read(ctx)
-        tmax = torch.tensor([t], dtype=torch.float64, device="cuda")
-        if world > 1:
-            dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        results[name] = dict(t=float(tmax.item()), stats=stats, launches=launches, prof=prof, clocks=clk.summary())
+        results[name] = dict(t=reduce_max(t, world), stats=stats, launches=launches, prof=prof,
+                             clocks=clk.summary())
 
     # end-to-end through the host-buffer entry point (mixed form)
     sim.precision = PRECISION_MIXED
@@ -338,11 +352,7 @@ def main(args):
         n, _ = sim.update_host(dt, pos_np[:n], vel_np[:n], ids_np[:n])
         d2h += n * 28
     ctx.synchronize()
-    te = time.perf_counter() - t0
-    tte = torch.tensor([te], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(tte, op=dist.ReduceOp.MAX)
-    te = float(tte.item())
+    te = reduce_max(time.perf_counter() - t0, world)
 
     if r == 0:
         mixed, plain = results["mixed"], results["plain"]

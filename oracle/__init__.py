@@ -77,6 +77,10 @@ def lib():
                                       _f32p, _i64, _f32p]
         L.gfo_advect_rk4.argtypes = [_i, _i, _i, _d, _f32p, _f32p, _f32p, _d, _f32p, _i64, _f32p]
         L.gfo_resolve_collisions.argtypes = [_i, _i, _i, _d, _u8p, _f32p, _i64, _f32p]
+        L.gfo_segment_voxel.argtypes = [_f32p, _f32p, _d, _i, _i, _i, _u8p, _i32p]
+        L.gfo_segment_voxel.restype = _i
+        L.gfo_ray_aabb.argtypes = [_f32p, _f32p, _f32p, _f32p, _f32p]
+        L.gfo_ray_aabb.restype = _i
         L.gfo_update_fluid_cells.argtypes = [_i, _i, _i, _d, _u8p, _f32p, _f32p, _u32p, _i64]
         L.gfo_update_fluid_cells.restype = _i64
         L.gfo_cap_particles_per_cell.argtypes = [_i, _i, _i, _d, _i, _f32p, _f32p, _u32p, _i64]

@@ -833,6 +833,15 @@ static void resolve_one(int ni, int nj, int nk, double dx, const uint8_t *mat,
     memcpy(p1, res, 3 * sizeof(float));
 }
 
+int gfo_segment_voxel(const float *p0, const float *p1, double dx, int ni, int nj, int nk,
+                      const uint8_t *mat, int *voxel) {
+    return segment_voxel(p0, p1, dx, mat, ni, nj, nk, voxel);
+}
+
+int gfo_ray_aabb(const float *p0, const float *dir, const float *bmin, const float *bmax, float *out) {
+    return ray_aabb(p0, dir, bmin, bmax, out);
+}
+
 void gfo_resolve_collisions(int ni, int nj, int nk, double dx, const uint8_t *mat,
                             const float *p0, int64_t n, float *p1) {
     for (int64_t p = 0; p < n; p++) {

@@ -118,6 +118,14 @@ void gfo_advect_rk4(int ni, int nj, int nk, double dx, const float *u, const flo
 void gfo_resolve_collisions(int ni, int nj, int nk, double dx, const uint8_t *mat,
                             const float *p0, int64_t n, float *p1);
 
+/* Collision::getLineSegmentVoxelIntersection (collision.cpp:303-402): 1 and the
+   first solid voxel on the segment p0 -> p1, or 0. */
+int gfo_segment_voxel(const float *p0, const float *p1, double dx, int ni, int nj, int nk,
+                      const uint8_t *mat, int *voxel);
+
+/* Collision::rayIntersectsAABB (collision.cpp:404-449) for the box [bmin, bmax]. */
+int gfo_ray_aabb(const float *p0, const float *dir, const float *bmin, const float *bmax, float *out);
+
 /* FluidSimulation::_removeMarkerParticlesInSolidCells (fluidsimulation.cpp:1933-1958)
    followed by _updateFluidCells' reclassification (:1990-2041).  Compacts the
    particle arrays in place (order kept) and returns the surviving count. */

@@ -1,0 +1,53 @@
+"""The C ABI on the CPU: libgfs.so builds for sm_103a, loads, and exports every
+entry point include/gfs.h declares; host-only calls behave (no GPU needed)."""
+import ctypes
+import os
+import re
+import shutil
+
+import pytest
+
+from gridfluidsim3d_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gfs.h")
+
+
+def _declared():
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+char\s*\*|int)\s*(gfs_\w+)\s*\(", src, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not shutil.which("nvcc") and not os.path.exists("/usr/local/cuda/bin/nvcc"):
+        pytest.skip("no CUDA toolkit")
+    from gridfluidsim3d_gb300 import build
+    build.build()
+    return _lib.load()
+
+
+def test_header_and_binding_agree():
+    assert _declared() == sorted(_lib.EXPORTS)
+
+
+def test_every_declared_symbol_is_exported(lib):
+    for name in _declared():
+        assert hasattr(lib, name), name
+
+
+def test_host_only_calls(lib):
+    assert lib.gfs_version().decode().startswith("gfs-gb300")
+    p = _lib.SimParams()
+    lib.gfs_sim_default_params(ctypes.byref(p))
+    assert p.density == 20.0 and p.max_cg_iterations == 200 and abs(p.ratio_pic - 0.05) < 1e-8
+    assert p.tol == 1e-6 and p.max_particles_per_cell == 100 and tuple(p.gravity) == (0.0, -25.0, 0.0)
+
+
+def test_errors_are_reported_not_raised(lib):
+    # a NULL out-pointer is rejected with a message, whatever the device situation
+    with pytest.raises(_lib.GFSError) as e:
+        lib.gfs_ctx_create(0, None)
+    assert "NULL" in str(e.value)
+    with pytest.raises(_lib.GFSError):
+        lib.gfs_sim_default_params(None)
