@@ -705,6 +705,203 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1) k_sweep(SweepArgs<T> A) {
     }
 }
 
+// Lean triangular solve (FWD / BWD).  One pencil per thread; everything that
+// does not depend on the step is hoisted, per-step addresses are pointer
+// increments, every slot of the block's plane is copied and stored (slots of
+// cells outside the grid store 0, which they already hold), and only the value
+// select, the dot product and the exchange words are predicated on the cell
+// being inside the grid.  This keeps the per-step instruction count -- the issue-rate limit of
+// the SMs hosting two such CTAs -- low.
+template <class T, int MODE, int P, int PE>
+__global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
+    using Op = Ar<T>;
+    using X = Xch<T>;
+    static_assert(MODE == SW_FWD || MODE == SW_BWD, "triangular solves only");
+    constexpr bool bwd = MODE == SW_BWD;
+    constexpr long long PS = bwd ? -(long long)SPLANE : (long long)SPLANE;
+    constexpr long long XP = (long long)XCH_PER_PLANE * X::W;
+    constexpr long long XS = bwd ? -XP : XP;
+    constexpr int NARR = bwd ? 3 : 2;
+    __shared__ T xb[2][SBK][SBJ];
+    __shared__ __align__(16) T ring[NARR][P][SPLANE];
+    __shared__ unsigned sh_ticket, sh_epoch;
+    if (A.ctrl->done) return;
+    const int tid = threadIdx.x;
+    const Skew &K = A.K;
+    const int S = K.S;
+    if (tid == 0) {
+        sh_ticket = atomicAdd(A.ticket, 1u);
+        sh_epoch = A.ctrl->epoch;
+    }
+    __syncthreads();
+    const unsigned t = sh_ticket, tag = sh_epoch;
+    int bj = (int)(t % K.nbj), bk = (int)(t / K.nbj);
+    if (bwd) {
+        bj = K.nbj - 1 - bj;
+        bk = K.nbk - 1 - bk;
+    }
+    const int pbj = bwd ? bj + 1 : bj - 1, pbk = bwd ? bk + 1 : bk - 1;
+    const int cbj = bwd ? bj - 1 : bj + 1, cbk = bwd ? bk - 1 : bk + 1;
+    const bool has_pj = pbj >= 0 && pbj < K.nbj, has_pk = pbk >= 0 && pbk < K.nbk;
+    const bool has_cj = cbj >= 0 && cbj < K.nbj, has_ck = cbk >= 0 && cbk < K.nbk;
+    bool timed_out = false;
+
+    const int jl = tid % SBJ, kl = tid / SBJ;
+    const bool valid = bj * SBJ + jl < K.ny && bk * SBK + kl < K.nz;
+    const int xj = bwd ? jl + 1 : jl - 1, xk = bwd ? kl + 1 : kl - 1;
+    const bool at_j = bwd ? jl == SBJ - 1 : jl == 0;
+    const bool at_k = bwd ? kl == SBK - 1 : kl == 0;
+    const bool in_j = at_j && has_pj, in_k = at_k && has_pk;
+    const bool out_j = (bwd ? jl == 0 : jl == SBJ - 1) && has_cj;
+    const bool out_k = (bwd ? kl == 0 : kl == SBK - 1) && has_ck;
+    const int st_lo = valid ? (bwd ? S - K.nx - jl - kl : jl + kl) : S;
+    const int st_hi = valid ? st_lo + K.nx : S;
+    const long long q0 = K.base(bj, bk) + kl * SBJ + jl + (bwd ? (long long)(S - 1) * SPLANE : 0);
+    // input pointers at step P (the first refill), output pointer at step 0
+    const T *fa = A.in + q0 + P * PS;
+    const T *fb = A.precon + q0 + P * PS;
+    const T *fc = (bwd ? A.rdot : A.in) + q0 + P * PS;
+    T *po = A.out + q0;
+    const long long xblock = (long long)S * XP;
+    unsigned long long *xbuf = A.xch;
+    unsigned long long *pxj_out = xbuf + (long long)(bk * K.nbj + bj) * xblock + (bwd ? (long long)(S - 1) * XP : 0) +
+                                  (long long)kl * X::W;
+    unsigned long long *pxk_out = xbuf + (long long)(bk * K.nbj + bj) * xblock + (bwd ? (long long)(S - 1) * XP : 0) +
+                                  (long long)(SBJ + jl) * X::W;
+    const unsigned long long *pxj_in =
+        xbuf + (has_pj ? (long long)(bk * K.nbj + pbj) * xblock +
+                             (bwd ? (long long)(S - 1 - (SBJ - 1)) : (long long)(SBJ - 1)) * XP + (long long)kl * X::W
+                       : 0);
+    const unsigned long long *pxk_in =
+        xbuf + (has_pk ? (long long)(pbk * K.nbj + bj) * xblock +
+                             (bwd ? (long long)(S - 1 - (SBK - 1)) : (long long)(SBK - 1)) * XP +
+                             (long long)(SBJ + jl) * X::W
+                       : 0);
+
+    // fill the ring with steps 0..P-1
+#pragma unroll
+    for (int u = 0; u < P; u++) {
+        if (u < S) {
+            cp_async<sizeof(T)>(&ring[0][u][tid], A.in + q0 + u * PS, true);
+            cp_async<sizeof(T)>(&ring[1][u][tid], A.precon + q0 + u * PS, true);
+            if (bwd) cp_async<sizeof(T)>(&ring[NARR - 1][u][tid], A.rdot + q0 + u * PS, true);
+        }
+        cp_async_commit();
+    }
+    unsigned long long r_wj[PE][X::W], r_wk[PE][X::W];
+#pragma unroll
+    for (int v = 0; v < PE; v++) {
+        const bool ok = v >= st_lo && v < st_hi;
+        if (in_j && ok) Xch<T>::fetch(pxj_in + v * XS, r_wj[v]);
+        if (in_k && ok) Xch<T>::fetch(pxk_in + v * XS, r_wk[v]);
+    }
+
+    T prev = T(0);
+    Acc2f dot32;
+    double dot64 = 0.0;
+    static_assert(P % PE == 0, "exchange ring must divide the input ring");
+    const int SP = ((S + P - 1) / P) * P;
+    for (int s0 = 0; s0 < SP; s0 += P) {
+#pragma unroll
+        for (int u = 0; u < P; u++) {
+            const int st = s0 + u;
+            const int v = u % PE;
+            cp_async_wait<P - 1>();
+            const bool act = st >= st_lo && st < st_hi;
+            T nj_ = at_j ? T(0) : xb[(st - 1) & 1][kl][xj];
+            T nk_ = at_k ? T(0) : xb[(st - 1) & 1][xk][jl];
+            if (in_j && act) nj_ = xch_take<T>(r_wj[v], pxj_in + (long long)st * XS, tag, A.ctrl, timed_out);
+            if (in_k && act) nk_ = xch_take<T>(r_wk[v], pxk_in + (long long)st * XS, tag, A.ctrl, timed_out);
+            const T ra = ring[0][u][tid], pc = ring[1][u][tid];
+            T val, xch;
+            if (MODE == SW_FWD) {
+                // _applyPreconditioner forward solve (pressuresolver.cpp:311-351); neighbours hand
+                // over (negscale*precon)*q; precon is 0 off the fluid set, so those cells give 0
+                val = Op::mul(Op::sub(Op::sub(Op::sub(ra, prev), nj_), nk_), pc);
+                xch = Op::mul(Op::mul(A.negscale, pc), val);
+            } else {
+                // backward solve (pressuresolver.cpp:354-385)
+                const T m = Op::mul(A.negscale, pc);
+                val = Op::mul(Op::sub(Op::sub(Op::sub(ra, Op::mul(m, prev)), Op::mul(m, nj_)), Op::mul(m, nk_)), pc);
+                xch = val;
+            }
+            // slots outside the grid (and steps past the last plane) store and hand over 0
+            val = act ? val : T(0);
+            xch = act ? xch : T(0);
+            if (MODE == SW_BWD && act) {
+                const T rv = ring[NARR - 1][u][tid];
+                if (sizeof(T) == 4) dot32.add((float)val * (float)rv);
+                else dot64 += (double)val * (double)rv;
+            }
+            if (st < S) {
+                *po = val;
+                if (out_j && act) X::put(pxj_out, xch, tag);
+                if (out_k && act) X::put(pxk_out, xch, tag);
+            }
+            po += PS;
+            pxj_out += XS;
+            pxk_out += XS;
+            xb[st & 1][kl][jl] = xch;
+            prev = xch;
+            // refill this slot with step st + P
+            if (st + P < S) {
+                cp_async<sizeof(T)>(&ring[0][u][tid], fa, true);
+                cp_async<sizeof(T)>(&ring[1][u][tid], fb, true);
+                if (bwd) cp_async<sizeof(T)>(&ring[NARR - 1][u][tid], fc, true);
+            }
+            cp_async_commit();
+            fa += PS;
+            fb += PS;
+            fc += PS;
+            {
+                const int sx = st + PE;
+                const bool ok = sx >= st_lo && sx < st_hi;
+                if (in_j && ok) Xch<T>::fetch(pxj_in + (long long)sx * XS, r_wj[v]);
+                if (in_k && ok) Xch<T>::fetch(pxk_in + (long long)sx * XS, r_wk[v]);
+            }
+            __syncthreads();
+        }
+    }
+    cp_async_wait<0>();
+
+    double part = 0.0;
+    if (MODE == SW_BWD) part = block_reduce<0>(sizeof(T) == 4 ? dot32.value() : dot64);
+    __shared__ bool last;
+    const unsigned nblocks = (unsigned)(K.nbj * K.nbk);
+    if (tid == 0) {
+        if (MODE == SW_BWD) A.partials[bj + K.nbj * bk] = part;
+        __threadfence();
+        unsigned tk = atomicAdd(A.done_ticket, 1u);
+        last = tk == nblocks - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (MODE == SW_BWD) {
+        double acc = 0.0;
+        for (unsigned q = tid; q < nblocks; q += SPLANE) acc += __ldcg(A.partials + q);
+        acc = block_reduce<0>(acc);
+        if (tid == 0) {
+            PsCtrl *C = A.ctrl;
+            if (A.init) {
+                C->sigma = acc;
+                C->beta = 0.0;
+            } else {
+                // _solvePressureSystem (pressuresolver.cpp:481-486)
+                C->beta = acc / C->sigma;
+                C->sigma = acc;
+                C->iter += 1;
+                if (C->iter >= C->max_iters) C->done = 1;
+            }
+        }
+    }
+    if (tid == 0) {
+        *A.ticket = 0;
+        *A.done_ticket = 0;
+        A.ctrl->epoch = tag + 1 == 0 ? 1u : tag + 1;
+    }
+}
+
 // -------------------------------------------------------- vector kernels
 
 template <class T>
@@ -936,7 +1133,10 @@ static int launch_sweep(Ctx *ctx, PressureWs &ws, const T *in, T *out, const T *
     A.ctrl = C;
     A.init = init;
     ProfScope prof(ctx, MODE == SW_FWD ? KC_SWEEP_FWD : (MODE == SW_BWD ? KC_SWEEP_BWD : KC_PRECON));
-    k_sweep<T, MODE, P, PE><<<A.K.nbj * A.K.nbk, SWEEP_THREADS, 0, ctx->stream>>>(A);
+    if (MODE == SW_PRECON)
+        k_sweep<T, MODE, P, PE><<<A.K.nbj * A.K.nbk, SWEEP_THREADS, 0, ctx->stream>>>(A);
+    else
+        k_tri<T, (MODE == SW_PRECON ? SW_FWD : MODE), P, PE><<<A.K.nbj * A.K.nbk, SPLANE, 0, ctx->stream>>>(A);
     ctx->launches++;
     GFS_LAUNCH_CHECK();
     return GFS_OK;
