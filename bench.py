@@ -59,6 +59,12 @@ BYTES = {
     ("g2p_advect", 0): 64, ("g2p_advect", 1): 64,   # read pos4+vel4, write pos4+vel4
 }
 
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# FP32 sweeps on this exact workload, from one ncu --set full capture of the
+# 5th/6th k_tri launches of this bench's mixed run.  The sweeps stream the whole dense
+# skewed grid, so the figure depends on the grid, not on the fluid-cell count.
+TRAFFIC = {"mic0_forward": 209.6e6, "mic0_backward": 292.7e6}
+
 
 def rank_info():
     r = int(os.environ.get("RANK", "0"))
@@ -317,7 +323,10 @@ def main(args):
     peak, peak_kind = load_peaks()
 
     results = {}
+    forms = [f for f in ("plain", "mixed") if f in args.forms.split(",")]
     for name, prec in (("plain", PRECISION_PLAIN), ("mixed", PRECISION_MIXED)):
+        if name not in forms:
+            continue
         sim.precision = prec
         reset(sim, sc)
         run_steps(sim, sc, args.warmup, dt)
@@ -343,18 +352,23 @@ def main(args):
     pos_np, vel_np, ids_np = hp.numpy(), hv.numpy(), hi.numpy().view(np.uint32)
     n = n0
     h2d = d2h = 0
-    for _ in range(args.warmup):
+    e2e_steps = 0 if args.no_e2e else args.steps
+    for _ in range(args.warmup if e2e_steps else 0):
         n, _ = sim.update_host(dt, pos_np[:n], vel_np[:n], ids_np[:n])
     barrier()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(e2e_steps):
         h2d += n * 28
         n, _ = sim.update_host(dt, pos_np[:n], vel_np[:n], ids_np[:n])
         d2h += n * 28
     ctx.synchronize()
     te = reduce_max(time.perf_counter() - t0, world)
 
-    if r == 0:
+    if r == 0 and set(forms) != {"plain", "mixed"}:
+        # partial run (profiling): report the timed forms only
+        print(json.dumps({k: {"ms_per_step": v["t"] / args.steps * 1e3, "gpu_launches": int(v["launches"])}
+                          for k, v in results.items()}), flush=True)
+    elif r == 0:
         mixed, plain = results["mixed"], results["plain"]
         value = world * args.steps / mixed["t"]
         # dominant kernel class of the timed mixed region
@@ -381,7 +395,8 @@ def main(args):
             roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                     "frac": achieved / peak, "peak_kind": f"{peak_kind} hbm_gbs",
                     "bytes_per_launch": bpu * unit_count, "avg_launch_ms": avg_s * 1e3,
-                    "working_launches": working, "traffic": None}
+                    "working_launches": working, "traffic": TRAFFIC.get(dom),
+                    "traffic_source": "ncu capture of this workload" if dom in TRAFFIC else None}
         breakdown = {k: round(v[0] / args.steps, 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0]) if v[0] > 0}
         pbreak = {k: round(v[0] / args.steps, 3) for k, v in sorted(plain["prof"].items(), key=lambda kv: -kv[1][0]) if v[0] > 0}
         plain_rate = world * args.steps / plain["t"]
@@ -417,8 +432,9 @@ def main(args):
                       "max_residual": [s["cg_max_residual"] for s in st],
                       "ms_per_stage": breakdown},
             "mixed_over_plain": value / plain_rate,
-            "e2e": {"value": world * args.steps / te, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
-                    "d2h_bytes_per_step": d2h // args.steps},
+            "e2e": (None if args.no_e2e else
+                    {"value": world * args.steps / te, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
+                     "d2h_bytes_per_step": d2h // args.steps}),
             "gpu_launches": int(mixed["launches"]),
             "roofline": roof,
             "cpu_baseline": cpu,
@@ -438,6 +454,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gfs", "reference"], default="gfs")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--forms", default="plain,mixed",
+                    help="pressure forms to time (a partial set prints a short line; for profiling)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     ap.add_argument("--ref-cg-iterations", type=int, default=200,
                     help="CG iterations the reference arm scales its per-iteration cost to")
     a = ap.parse_args()

@@ -56,6 +56,7 @@ def _compile(src: str, extra: list[str]) -> str:
 def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     extra = ["-Xptxas", "-v"] if ptxas_info else []
+    extra += os.environ.get("GFS_NVCC_EXTRA", "").split()   # e.g. tuning macros (-DGFS_SWEEP_PE=4)
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), srcs))

@@ -360,6 +360,13 @@ __device__ __forceinline__ T mic0_precon(unsigned nb, uint8_t fl, T pim1, T pjm1
 // whose tag equals the current epoch holds the producer's value for this sweep:
 // no progress counters and no memory fences are needed.  FP64 values travel as
 // two tagged words.
+// L2 load that the compiler keeps where it is written (polls and prefetches of
+// exchange words must not be merged, hoisted out of a loop or sunk to their use)
+__device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.global.cg.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
 template <class T> struct Xch;
 template <> struct Xch<float> {
     static constexpr int W = 1;
@@ -368,7 +375,7 @@ template <> struct Xch<float> {
         __stcg(p, w);
     }
     static __device__ __forceinline__ void fetch(const unsigned long long *p, unsigned long long w[1]) {
-        w[0] = __ldcg(p);
+        w[0] = ld_cg_u64(p);
     }
     static __device__ __forceinline__ bool ready(const unsigned long long w[1], unsigned tag) {
         return (unsigned)(w[0] >> 32) == tag;
@@ -385,8 +392,8 @@ template <> struct Xch<double> {
         __stcg(p + 1, ((unsigned long long)tag << 32) | (bits >> 32));
     }
     static __device__ __forceinline__ void fetch(const unsigned long long *p, unsigned long long w[2]) {
-        w[0] = __ldcg(p);
-        w[1] = __ldcg(p + 1);
+        w[0] = ld_cg_u64(p);
+        w[1] = ld_cg_u64(p + 1);
     }
     static __device__ __forceinline__ bool ready(const unsigned long long w[2], unsigned tag) {
         return (unsigned)(w[0] >> 32) == tag && (unsigned)(w[1] >> 32) == tag;
@@ -463,11 +470,6 @@ __device__ __forceinline__ void tma_load_1d(void *dst, const void *src, unsigned
 }
 
 // Exchange words are read with an in-place L2 load (asm volatile keeps it where it is written).
-__device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long *p) {
-    unsigned long long v;
-    asm volatile("ld.global.cg.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
 
 // In-place loads for the wavefront's prefetch ring: asm volatile keeps each load
 // where it is written (P steps before its use), so its latency overlaps the
@@ -1108,7 +1110,13 @@ static int ensure_ws(Ctx *ctx, PressureWs &ws, const Grids &g, bool mixed) {
     return GFS_OK;
 }
 
-template <class T, int MODE, int P = (sizeof(T) == 8 ? 4 : 8), int PE = 2>
+// PE: how many steps ahead a pencil on a block edge loads the upstream block's
+// exchange words (the L2 round trip must fit in PE steps)
+#ifndef GFS_SWEEP_PE
+#define GFS_SWEEP_PE 4
+#endif
+template <class T, int MODE, int P = (sizeof(T) == 8 ? 4 : 8),
+          int PE = (GFS_SWEEP_PE < P ? GFS_SWEEP_PE : P)>
 static int launch_sweep(Ctx *ctx, PressureWs &ws, const T *in, T *out, const T *precon, const T *rdot,
                         float *out32, double scale, int init) {
     SweepArgs<T> A;
