@@ -67,7 +67,7 @@ _SIGNATURES = {
     "gfs_ctx_profile_enable": [_P, _I],
     "gfs_ctx_profile_reset": [_P],
     "gfs_ctx_profile_read": [_P, _I, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_D), ctypes.POINTER(_I64)],
-    "gfs_scalar_field_add_point_values": [_P, _P, _P, _I64, _D, _P, _D, _I, _I, _I, _P, _P],
+    "gfs_scalar_field_add_point_values": [_P, _P, _P, _I64, _D, _P, _D, _I, _I, _I, _P, _P, _I, _D],
     "gfs_velocity_scalar_field": [_P, _I, _I, _I, _I, _D, _P, _P, _I64, _P, _P],
     "gfs_tricubic_interpolate": [_P, _I, _I, _I, _D, _P, _P, _P, _P, _I64, _P],
     "gfs_advect_particles": [_P, _I, _I, _I, _I, _D, _P, _P, _P, _D, _P, _I64, _P],

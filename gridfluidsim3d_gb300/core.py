@@ -122,30 +122,94 @@ class MACVelocityField:
 
 
 class CLScalarField:
-    """Splat accelerator (CLScalarField, clscalarfield.h:67-125), CUDA backed."""
+    """Splat accelerator (CLScalarField, clscalarfield.h:67-125), CUDA backed.
+
+    Methods keep the reference's names in snake case.  The device/work-load
+    toggles of the reference's OpenCL path are kept for source compatibility;
+    disable_opencl() leaves no backend (there is no CPU path here), so compute
+    calls then raise instead of silently running something else."""
 
     def __init__(self, ctx: Context | None = None):
         self.ctx = ctx or Context.default()
         self._initialized = False
+        self._enabled = True
+        self._thr = None
+        self._workload = 10000
 
     def initialize(self) -> bool:
         self._initialized = True
         return True
 
-    def add_point_values(self, points, values, radius, offset, dx, scalarfield, weightfield=None):
-        """Add sum(w*v) into scalarfield (and sum(w) into weightfield) for every node
-        within `radius` of point - offset (clscalarfield.cpp:200-267)."""
+    # -- CLScalarField::setMaxScalarFieldValueThreshold & co (clscalarfield.cpp:303-318)
+    def set_max_scalar_field_value_threshold(self, val: float | None = None):
+        self._thr = None if val is None else float(np.float32(val))
+
+    def is_max_scalar_field_value_threshold_set(self) -> bool:
+        return self._thr is not None
+
+    def get_max_scalar_field_value_threshold(self) -> float:
+        return 0.0 if self._thr is None else self._thr
+
+    # -- device toggles (clscalarfield.cpp:320-517)
+    def enable_opencl(self):
+        self._enabled = True
+
+    def disable_opencl(self):
+        self._enabled = False
+
+    def is_opencl_enabled(self) -> bool:
+        return self._enabled
+
+    def is_using_gpu(self) -> bool:
+        return self._enabled
+
+    def is_using_cpu(self) -> bool:
+        return False
+
+    def get_device_info(self) -> str:
+        return self.ctx.device_name()
+
+    def get_kernel_work_load_size(self) -> int:
+        return self._workload
+
+    def set_kernel_work_load_size(self, n: int):
+        self._workload = int(n)
+
+    def _check(self, func):
+        if not self._enabled:
+            raise GFSError(_lib.GFS_ERR_STATE, func, "accelerator disabled (disable_opencl); no CPU path is provided")
+
+    def _splat(self, func, points, values, radius, offset, dx, field, weight):
+        self._check(func)
         pts = _arr(points, np.float32).reshape(-1, 3)
-        vals = _arr(values, np.float32)
-        if len(vals) != len(pts):
-            raise GFSError(_lib.GFS_ERR_INVALID, "add_point_values", "points and values differ in length")
-        if scalarfield.dtype != np.float32 or not scalarfield.flags.c_contiguous:
-            raise GFSError(_lib.GFS_ERR_INVALID, "add_point_values", "scalarfield must be contiguous float32")
-        D, H, W = scalarfield.shape
+        vals = None
+        if values is not None:
+            vals = _arr(values, np.float32)
+            if len(vals) != len(pts):
+                raise GFSError(_lib.GFS_ERR_INVALID, func, "points and values differ in length")
+        for name, a in (("field", field), ("weightfield", weight)):
+            if a is not None and (a.dtype != np.float32 or not a.flags.c_contiguous or a.ndim != 3):
+                raise GFSError(_lib.GFS_ERR_INVALID, func, f"{name} must be a contiguous 3-D float32 array")
+        if weight is not None and weight.shape != field.shape:
+            raise GFSError(_lib.GFS_ERR_INVALID, func, "scalarfield and weightfield differ in shape")
+        D, H, W = field.shape
         off = _arr(offset, np.float32)
-        _lib.lib().gfs_scalar_field_add_point_values(self.ctx.handle, _p(pts), _p(vals), len(pts), float(radius),
-                                                     _p(off), float(dx), W, H, D, _p(scalarfield),
-                                                     _p(weightfield) if weightfield is not None else None)
+        thr = self._thr
+        _lib.lib().gfs_scalar_field_add_point_values(
+            self.ctx.handle, _p(pts), _p(vals) if vals is not None else None, len(pts), float(radius), _p(off),
+            float(dx), W, H, D, _p(field), _p(weight) if weight is not None else None, int(thr is not None),
+            float(thr or 0.0))
+
+    def add_points(self, points, radius, offset, dx, field):
+        """CLScalarField::addPoints (clscalarfield.cpp:68-122): field += w for every
+        node within `radius` of point - offset.  `field` is updated in place."""
+        self._splat("add_points", points, None, radius, offset, dx, field, None)
+
+    def add_point_values(self, points, values, radius, offset, dx, scalarfield, weightfield=None):
+        """CLScalarField::addPointValues (clscalarfield.cpp:144-267): scalarfield +=
+        w*v (and weightfield += w) for every node within `radius` of point - offset.
+        The arrays are updated in place."""
+        self._splat("add_point_values", points, values, radius, offset, dx, scalarfield, weightfield)
 
     def velocity_scalar_field(self, dir_, isize, jsize, ksize, dx, positions, velocities):
         """FluidSimulation::_computeVelocityScalarField for one MAC component:

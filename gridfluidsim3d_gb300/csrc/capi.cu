@@ -754,12 +754,38 @@ int gfs_pressure_solve(gfs_ctx *ctx, int ni, int nj, int nk, double dx, double d
 
 int gfs_scalar_field_add_point_values(gfs_ctx *ctx, const float *h_points, const float *h_values, int64_t n,
                                       double radius, const float offset[3], double dx, int W, int H, int D,
-                                      float *h_scalarfield, float *h_weightfield) {
+                                      float *h_scalarfield, float *h_weightfield, int threshold_set,
+                                      double threshold) {
     GFS_NONNULL(ctx);
-    (void)h_points; (void)h_values; (void)n; (void)radius; (void)offset; (void)dx;
-    (void)W; (void)H; (void)D; (void)h_scalarfield; (void)h_weightfield;
-    set_error(GFS_ERR_STATE, "gfs_scalar_field_add_point_values: general-radius splat not available yet");
-    return GFS_ERR_STATE;
+    GFS_NONNULL(offset);
+    GFS_NONNULL(h_scalarfield);
+    const long long nodes = (long long)W * H * D;
+    if (W <= 0 || H <= 0 || D <= 0 || nodes >= 0xFFFFFFFFll || !(dx > 0) || !(radius > 0) ||
+        !std::isfinite(radius) || n < 0 || n > 0x7FFFFFFFll || (n > 0 && !h_points)) {
+        set_error(GFS_ERR_INVALID, "invalid point splat arguments (W=%d H=%d D=%d dx=%g radius=%g n=%lld)", W, H, D,
+                  dx, radius, (long long)n);
+        return GFS_ERR_INVALID;
+    }
+    if (n == 0) return GFS_OK;
+    Ctx *c = &ctx->c;
+    DevMem dp, dv, df, dw;
+    const size_t fbytes = (size_t)nodes * sizeof(float);
+    if (dp.alloc((size_t)n * 3 * sizeof(float)) || (h_values && dv.alloc((size_t)n * sizeof(float))) ||
+        df.alloc(fbytes) || (h_weightfield && dw.alloc(fbytes)))
+        return GFS_ERR_NOMEM;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(dp.p, h_points, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    if (h_values)
+        GFS_CUDA_CHECK(cudaMemcpyAsync(dv.p, h_values, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    GFS_CUDA_CHECK(cudaMemcpyAsync(df.p, h_scalarfield, fbytes, cudaMemcpyHostToDevice, c->stream));
+    if (h_weightfield) GFS_CUDA_CHECK(cudaMemcpyAsync(dw.p, h_weightfield, fbytes, cudaMemcpyHostToDevice, c->stream));
+    int rc = splat_points(c, dp.as<float>(), h_values ? dv.as<float>() : nullptr, n, radius, offset, dx, W, H, D,
+                          df.as<float>(), h_weightfield ? dw.as<float>() : nullptr, threshold_set != 0,
+                          (float)threshold);
+    if (rc) return rc;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(h_scalarfield, df.p, fbytes, cudaMemcpyDeviceToHost, c->stream));
+    if (h_weightfield) GFS_CUDA_CHECK(cudaMemcpyAsync(h_weightfield, dw.p, fbytes, cudaMemcpyDeviceToHost, c->stream));
+    GFS_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+    return GFS_OK;
 }
 
 }  // extern "C"

@@ -141,11 +141,13 @@ size_t scan_temp_elems(long long n);
 // ---- splat.cu
 int splat_velocity(Sim *s);           // P2G for U, V, W into sval/smask
 int face_fill(Sim *s, double dt);     // a3 + saved copy + body forces
-// standalone weighted splat on an arbitrary node grid (device buffers)
-int splat_points_device(Ctx *ctx, const float4 *pos, const float *vals, const uint32_t *offsets,
-                        const uint32_t *perm, int cni, int cnj, int cnk, double cdx,
-                        double radius, const float offset[3], double dx, int W, int H, int D,
-                        float *field, float *weight, float *vfield, uint8_t *vmask, bool normalise);
+
+// ---- pointsplat.cu
+// General weighted point splat on a W x H x D node grid (device buffers; d_vals
+// NULL = value 1, d_weight may be NULL).  Adds into d_field / d_weight.
+int splat_points(Ctx *ctx, const float *d_pts, const float *d_vals, long long n, double radius,
+                 const float offset[3], double dx, int W, int H, int D, float *d_field, float *d_weight,
+                 bool thr_set, float thr);
 
 // ---- extrapolate.cu
 int build_layers(Sim *s, int num_layers);

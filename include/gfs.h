@@ -71,21 +71,27 @@ int gfs_ctx_device_name(gfs_ctx *ctx, char *buf, int buflen);
 
 /* ------------------------------------------- splat (CLScalarField drop-in) */
 
-/* Weighted point splat: for every point p with value v, every grid node x within
-   `radius` of p - offset receives  field += w*v  and  weight += w  with
-   w = 1 - 4/9 s^3 + 17/9 s^2 - 22/9 s, s = |x - p|^2 / radius^2.
+/* Weighted point splat: for every point p with value v and every grid node x
+   (node (i,j,k) sits at (i,j,k)*dx) inside the index bounds of p - offset
+   (Grid3d::getGridIndexBounds, grid3d.h:350-371) and strictly within `radius`:
+       field += w*v,  weight += w,   w = 1 - 4/9 s^3 + 17/9 s^2 - 22/9 s,
+       s = |x - (p - offset)|^2 / radius^2
+   (ScalarField::addPoint / addPointValue, scalarfield.cpp:121-201).
    Replaces CLScalarField::addPointValues(points, values, radius, offset, dx,
-   scalarfield, weightfield) (clscalarfield.h:84-90, clscalarfield.cpp:200-267)
-   and its kernel compute_scalar_field_weight_point_values
-   (kernels/scalarfield.cl:202-268).  Adds into the caller's arrays ("add"
-   semantics of the reference's accelerated path, clscalarfield.cpp:1413,1448).
-   h_weightfield may be NULL: then only field += w*v is formed
-   (addPointValues without weight field, clscalarfield.h:78-83).
-   Field dims W x H x D; node (i,j,k) sits at (i,j,k)*dx. */
+   scalarfield[, weightfield]) (clscalarfield.h:83-95, clscalarfield.cpp:144-267)
+   and, with h_values = NULL (v = 1), CLScalarField::addPoints(points, radius,
+   offset, dx, field) (clscalarfield.h:70-74, clscalarfield.cpp:68-122), and
+   their kernels (kernels/scalarfield.cl:79-268).  Adds into the caller's
+   arrays (the accelerated path's semantics, clscalarfield.cpp:1413,1448);
+   h_weightfield may be NULL (no weight field).  Field dims W x H x D, x fastest.
+   threshold_set != 0 applies CLScalarField::setMaxScalarFieldValueThreshold
+   (clscalarfield.cpp:303-318) per node: a node whose incoming value exceeds
+   `threshold` receives nothing.  Each node sums its contributions in a fixed
+   order, so the result does not depend on scheduling. */
 int gfs_scalar_field_add_point_values(gfs_ctx *ctx, const float *h_points, const float *h_values,
                                       int64_t n, double radius, const float offset[3], double dx,
                                       int W, int H, int D, float *h_scalarfield,
-                                      float *h_weightfield);
+                                      float *h_weightfield, int threshold_set, double threshold);
 
 /* Velocity splat of one MAC component: FluidSimulation::_computeVelocityScalarField
    (fluidsimulation.cpp:2526-2595): weighted splat of velocity[dir] with radius dx

@@ -60,6 +60,8 @@ def lib():
             build(ref=False)
         L = ctypes.CDLL(LIB_PATH)
         L.gfo_splat_add.argtypes = [_f32p, _f32p, _i64, _d, _f32p, _d, _i, _i, _i, _f32p, _f32p]
+        L.gfo_splat_points.argtypes = [_f32p, ctypes.c_void_p, _i64, _d, _f32p, _d, _i, _i, _i, _f32p,
+                                       ctypes.c_void_p, _i, _d]
         L.gfo_apply_weight.argtypes = [_i64, _f32p, _f32p]
         L.gfo_velocity_scalar_field.argtypes = [_i, _i, _i, _i, _d, _f32p, _f32p, _i64, _f32p, _u8p]
         L.gfo_advect_velocity_field.argtypes = [_i, _i, _i, _d, _u8p, _f32p, _f32p, _i64, _f32p, _f32p, _f32p]
@@ -102,6 +104,8 @@ def ref():
         if not os.path.exists(REF_PATH):
             build(ref=True)
         L = ctypes.CDLL(REF_PATH)
+        L.gfsref_add_point_values.argtypes = [_f32p, ctypes.c_void_p, _i64, _d, _f32p, _d, _i, _i, _i, _f32p,
+                                              ctypes.c_void_p, _i, _d]
         L.gfsref_velocity_scalar_field.argtypes = [_i, _i, _i, _i, _d, _f32p, _f32p, _i64, _f32p, _f32p]
         L.gfsref_pressure_solve.argtypes = [_i, _i, _i, _d, _d, _d, _u8p, _f32p, _f32p, _f32p, _f64p]
         L.gfsref_pressure_solve.restype = _i
@@ -234,7 +238,36 @@ def substep(dims, dx, dt, g, mat, pos, vel, ids, density=20.0, ratio_pic=float(n
                 cg_max_resid=st.cg_max_resid)
 
 
+def _splat_args(points, values, offset, field, weight):
+    pts = _c(points, np.float32).reshape(-1, 3)
+    vals = None if values is None else _c(values, np.float32)
+    off = _c(offset, np.float32)
+    f = _c(field, np.float32).copy()
+    w = None if weight is None else _c(weight, np.float32).copy()
+    D, H, W = f.shape
+    vp = None if vals is None else vals.ctypes.data_as(ctypes.c_void_p)
+    wp = None if w is None else w.ctypes.data_as(ctypes.c_void_p)
+    return pts, vals, off, f, w, (W, H, D), vp, wp
+
+
+def splat_points(points, values, radius, offset, dx, field, weight=None, threshold=None):
+    """CLScalarField::addPointValues (values given) / addPoints (values None) into
+    copies of field / weight; returns (field, weight)."""
+    pts, vals, off, f, w, (W, H, D), vp, wp = _splat_args(points, values, offset, field, weight)
+    lib().gfo_splat_points(pts, vp, len(pts), float(radius), off, float(dx), W, H, D, f, wp,
+                           int(threshold is not None), float(threshold or 0.0))
+    return f, w
+
+
 # ------------------------------------------------- reference shim wrappers
+
+def ref_add_point_values(points, values, radius, offset, dx, field, weight=None, threshold=None):
+    """The reference's ScalarField::addPoint / addPointValue on copies of field / weight."""
+    pts, vals, off, f, w, (W, H, D), vp, wp = _splat_args(points, values, offset, field, weight)
+    ref().gfsref_add_point_values(pts, vp, len(pts), float(radius), off, float(dx), W, H, D, f, wp,
+                                  int(threshold is not None), float(threshold or 0.0))
+    return f, w
+
 
 def ref_velocity_scalar_field(dir_, dims, dx, pos, vel):
     ni, nj, nk = dims

@@ -65,22 +65,25 @@ static inline void pos_to_cell(const float *p, double dx, int *i, int *j, int *k
 
 /* --------------------------------------------------------------- a2: splat */
 
-/* ScalarField::addPointValue (scalarfield.cpp:167-201) with the bounds of
-   Grid3d::getGridIndexBounds (grid3d.h:350-371) and the kernel of
-   ScalarField::_evaluateTricubicFieldFunctionForRadiusSquared (:569-571). */
-void gfo_splat_add(const float *pos, const float *val, int64_t n, double r,
-                   const float offset[3], double dx, int W, int H, int D,
-                   float *field, float *weight) {
+void gfo_splat_points(const float *pos, const float *val, int64_t n, double r,
+                      const float offset[3], double dx, int W, int H, int D,
+                      float *field, float *weight, int thr_set, double thr) {
     /* ScalarField::setPointRadius (scalarfield.cpp:38-44) */
     double coef1 = (4.0 / 9.0) * (1.0 / (r * r * r * r * r * r));
     double coef2 = (17.0 / 9.0) * (1.0 / (r * r * r * r));
     double coef3 = (22.0 / 9.0) * (1.0 / (r * r));
     double rsq = r * r;
     double inv = 1.0 / dx;
+    float *before = NULL;
+    float fthr = (float)thr;
+    if (thr_set) {
+        before = (float *)malloc((size_t)W * H * D * sizeof(float));
+        memcpy(before, field, (size_t)W * H * D * sizeof(float));
+    }
     for (int64_t pi = 0; pi < n; pi++) {
         /* p -= _gridOffset (float) */
         float p[3] = {pos[3 * pi] - offset[0], pos[3 * pi + 1] - offset[1], pos[3 * pi + 2] - offset[2]};
-        double scale = (double)val[pi];
+        double scale = val ? (double)val[pi] : 1.0;
         int ci, cj, ck;
         pos_to_cell(p, dx, &ci, &cj, &ck);
         /* cpos = vec3((float)c.i*dx, ...) -> float; trans = p - cpos (float) */
@@ -98,6 +101,8 @@ void gfo_splat_add(const float *pos, const float *val, int64_t n, double r,
         for (int k = k0; k <= k1; k++) {
             for (int j = j0; j <= j1; j++) {
                 for (int i = i0; i <= i1; i++) {
+                    int64_t f = idx3(i, j, k, W, H);
+                    if (thr_set && before[f] > fthr) continue;
                     /* gpos = Grid3d::GridIndexToPosition(i,j,k,dx) (grid3d.h:79-81) */
                     float gx = (float)((double)(float)i * dx);
                     float gy = (float)((double)(float)j * dx);
@@ -108,14 +113,24 @@ void gfo_splat_add(const float *pos, const float *val, int64_t n, double r,
                     double distsq = (double)d2f;
                     if (distsq < rsq) {
                         double wgt = 1.0 - coef1 * distsq * distsq * distsq + coef2 * distsq * distsq - coef3 * distsq;
-                        int64_t f = idx3(i, j, k, W, H);
                         field[f] += (float)(wgt * scale);
-                        weight[f] += (float)wgt;
+                        if (weight) weight[f] += (float)wgt;
                     }
                 }
             }
         }
     }
+    free(before);
+}
+
+/* ScalarField::addPointValue (scalarfield.cpp:167-201) with the bounds of
+   Grid3d::getGridIndexBounds (grid3d.h:350-371) and the kernel of
+   ScalarField::_evaluateTricubicFieldFunctionForRadiusSquared (:569-571),
+   weight field enabled. */
+void gfo_splat_add(const float *pos, const float *val, int64_t n, double r,
+                   const float offset[3], double dx, int W, int H, int D,
+                   float *field, float *weight) {
+    gfo_splat_points(pos, val, n, r, offset, dx, W, H, D, field, weight, 0, 0.0);
 }
 
 void gfo_apply_weight(int64_t count, float *field, const float *weight) {

@@ -39,6 +39,15 @@ void gfo_splat_add(const float *pos, const float *val, int64_t n, double radius,
                    const float offset[3], double dx, int W, int H, int D,
                    float *field, float *weight);
 
+/* CLScalarField::addPoints / addPointValues with add semantics: val NULL gives
+   v = 1 (ScalarField::addPoint, scalarfield.cpp:126-160), weight may be NULL
+   (no weight field).  thr_set != 0: a node whose value before the call exceeds
+   thr receives nothing (ScalarField's per-node threshold test,
+   scalarfield.cpp:141-143, applied to the incoming field). */
+void gfo_splat_points(const float *pos, const float *val, int64_t n, double radius,
+                      const float offset[3], double dx, int W, int H, int D,
+                      float *field, float *weight, int thr_set, double thr);
+
 /* ScalarField::applyWeightField (scalarfield.cpp:90-106). */
 void gfo_apply_weight(int64_t count, float *field, const float *weight);
 

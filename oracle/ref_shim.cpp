@@ -13,6 +13,10 @@
 //                                   (scalarfield.cpp:90-106,167-201), configured
 //                                   like FluidSimulation::_computeVelocityScalarField
 //                                   (fluidsimulation.cpp:2526-2595)
+//   gfsref_add_point_values      -> ScalarField::addPoint / addPointValue
+//                                   (scalarfield.cpp:126-201) onto a field that
+//                                   starts from the caller's values, optional
+//                                   weight field and max threshold
 //   gfsref_pressure_solve        -> PressureSolver::solve (pressuresolver.cpp:116)
 //   gfsref_evaluate_velocity     -> MACVelocityField::evaluateVelocityAtPosition
 //                                   (macvelocityfield.cpp:549)
@@ -78,6 +82,35 @@ void fill_mac(MACVelocityField &m, int ni, int nj, int nk, const float *u, const
 }  // namespace
 
 extern "C" {
+
+void gfsref_add_point_values(const float *pos, const float *val, int64_t n, double r, const float *offset,
+                             double dx, int W, int H, int D, float *field, float *weight, int thr_set,
+                             double thr) {
+    ScalarField sf(W, H, D, dx);
+    if (weight) sf.enableWeightField();
+    sf.setPointRadius(r);
+    sf.setOffset(vmath::vec3(offset[0], offset[1], offset[2]));
+    if (thr_set) sf.setMaxScalarFieldThreshold(thr);
+    Array3d<float> *fp = sf.getPointerToScalarField();
+    Array3d<float> *wp = weight ? sf.getPointerToWeightField() : nullptr;
+    for (int k = 0; k < D; k++)
+        for (int j = 0; j < H; j++)
+            for (int i = 0; i < W; i++) {
+                fp->set(i, j, k, field[i + W * (j + H * k)]);
+                if (wp) wp->set(i, j, k, weight[i + W * (j + H * k)]);
+            }
+    for (int64_t q = 0; q < n; q++) {
+        vmath::vec3 p(pos[3 * q], pos[3 * q + 1], pos[3 * q + 2]);
+        if (val) sf.addPointValue(p, (double)val[q]);
+        else sf.addPoint(p);
+    }
+    for (int k = 0; k < D; k++)
+        for (int j = 0; j < H; j++)
+            for (int i = 0; i < W; i++) {
+                field[i + W * (j + H * k)] = fp->get(i, j, k);
+                if (wp) weight[i + W * (j + H * k)] = wp->get(i, j, k);
+            }
+}
 
 void gfsref_velocity_scalar_field(int dir, int ni, int nj, int nk, double dx, const float *pos,
                                   const float *vel, int64_t n, float *field, float *weight) {

@@ -29,6 +29,28 @@ def fluid_state(sc):
     return mat, pos[:n], vel[:n], ids[:n]
 
 
+def point_splat_cases():
+    """Seeded inputs of the general point-splat fixture."""
+    rng = np.random.default_rng(51)
+    cases = []
+    for t, (rmul, with_vals, with_w, thr) in enumerate([(1.0, True, True, False), (1.5, True, False, False),
+                                                         (2.3, False, True, False), (0.7, False, False, False),
+                                                         (1.2, True, True, True), (1.0, False, True, True)]):
+        W, H, D = (int(x) for x in rng.integers(6, 13, 3))
+        dx = float(rng.uniform(0.1, 0.5))
+        n = int(rng.integers(200, 600))
+        pts = rng.uniform(-2 * dx, (max(W, H, D) + 2) * dx, (n, 3)).astype(np.float32)
+        field = np.zeros((D, H, W), np.float32)
+        if thr:
+            field = rng.uniform(0, 1, (D, H, W)).astype(np.float32)
+            field[rng.random((D, H, W)) < 0.4] = 100.0
+        cases.append(dict(points=pts, values=rng.normal(size=n).astype(np.float32) if with_vals else None,
+                          radius=rmul * dx, offset=rng.uniform(-dx, dx, 3).astype(np.float32), dx=dx,
+                          field=field, weight=np.zeros_like(field) if with_w else None,
+                          threshold=50.0 if thr else None))
+    return cases
+
+
 def main():
     O.build(ref=True)
     out = {}
@@ -76,6 +98,20 @@ def main():
         vox[q] = v3
     np.savez_compressed(os.path.join(HERE, "collision.npz"), dims=np.array(dims), dx=dx, mat=mat, p0=p0, p1=p1,
                         hit=hit, voxel=vox)
+    # 5. general point splat (ScalarField::addPoint / addPointValue, the CLScalarField
+    #    addPoints / addPointValues semantics): radii, offsets, no values, no weight
+    #    field, points outside the grid, and a max-value threshold over a preset field
+    d = {}
+    for t, case in enumerate(point_splat_cases()):
+        f, w = O.ref_add_point_values(case["points"], case.get("values"), case["radius"], case["offset"],
+                                      case["dx"], case["field"], case.get("weight"), case.get("threshold"))
+        for key, val in case.items():
+            if val is not None:
+                d[f"{t}_{key}"] = np.asarray(val)
+        d[f"{t}_out_field"] = f
+        if w is not None:
+            d[f"{t}_out_weight"] = w
+    np.savez_compressed(os.path.join(HERE, "point_splat.npz"), ncases=len(point_splat_cases()), **d)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -11,6 +11,8 @@ Tolerances (the reference's stated bars):
   * pressure (PLAIN, FP64): CG iteration count equal within +-1, pressure
     relative 1e-9 (only the dot-product summation order differs);
   * pressure (MIXED): FP64 max-norm residual below the reference tolerance 1e-6.
+  * general point splat (addPoints / addPointValues): relative 1e-5 with an
+    absolute floor of 1e-6 of the output's scale; the touched node set equal.
 """
 import numpy as np
 import pytest
@@ -57,6 +59,72 @@ def test_splat_empty_and_single(gpu_ctx, oracle_lib):
         of, os_ = O.velocity_scalar_field(d, dims, dx, pos, vel)
         assert np.array_equal(s, os_.astype(bool))
         np.testing.assert_allclose(f, of, rtol=1e-6, atol=1e-7)
+
+
+def _point_splat_gpu(acc, c):
+    f = c["field"].copy()
+    w = c["weight"].copy() if "weight" in c else None
+    acc.set_max_scalar_field_value_threshold(c.get("threshold"))
+    if "values" in c:
+        acc.add_point_values(c["points"], c["values"], c["radius"], c["offset"], c["dx"], f, w)
+    else:
+        if w is None:
+            acc.add_points(c["points"], c["radius"], c["offset"], c["dx"], f)
+        else:
+            # addPoints with a weight field: v = 1 for every point
+            acc.add_point_values(c["points"], np.ones(len(c["points"]), np.float32), c["radius"], c["offset"],
+                                 c["dx"], f, w)
+    return f, w
+
+
+def test_point_splat_matches_reference_fixture(gpu_ctx):
+    from test_oracle_golden import point_splat_cases
+    acc = CLScalarField(gpu_ctx)
+    for c in point_splat_cases():
+        f, w = _point_splat_gpu(acc, c)
+        ref = c["out_field"]
+        scale = max(float(np.abs(ref).max()), 1e-3)
+        assert np.array_equal(f != c["field"], ref != c["field"]), "touched node set differs"
+        np.testing.assert_allclose(f, ref, rtol=1e-5, atol=1e-6 * scale)
+        if w is not None:
+            np.testing.assert_allclose(w, c["out_weight"], rtol=1e-5, atol=1e-6 * max(float(c["out_weight"].max()), 1e-3))
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_point_splat_large(gpu_ctx, oracle_lib, seed):
+    O = oracle_lib
+    rng = np.random.default_rng(100 + seed)
+    W, H, D = 40, 33, 29
+    dx = 0.1
+    acc = CLScalarField(gpu_ctx)
+    acc.set_max_scalar_field_value_threshold(None)
+    for rmul in (1.0, 2.5):
+        n = 60000
+        pts = rng.uniform(-0.2, 4.2, (n, 3)).astype(np.float32)
+        vals = rng.normal(size=n).astype(np.float32)
+        off = np.array([0.0, 0.05, 0.05], np.float32)
+        f = np.zeros((D, H, W), np.float32)
+        w = np.zeros_like(f)
+        acc.add_point_values(pts, vals, rmul * dx, off, dx, f, w)
+        of, ow = O.splat_points(pts, vals, rmul * dx, off, dx, np.zeros_like(f), np.zeros_like(f))
+        assert np.array_equal(w > 0, ow > 0)
+        np.testing.assert_allclose(w, ow, rtol=1e-5, atol=1e-6 * float(ow.max()))
+        np.testing.assert_allclose(f, of, rtol=1e-5, atol=1e-5 * float(np.abs(of).max()))
+
+
+def test_point_splat_edge_cases(gpu_ctx):
+    acc = CLScalarField(gpu_ctx)
+    f = np.full((4, 5, 6), 0.25, np.float32)
+    acc.add_points(np.zeros((0, 3), np.float32), 0.3, (0, 0, 0), 0.1, f)
+    assert (f == 0.25).all()
+    # points far outside the grid reach nothing
+    acc.add_points(np.array([[50.0, 50.0, 50.0], [-9.0, 0.1, 0.1]], np.float32), 0.3, (0, 0, 0), 0.1, f)
+    assert (f == 0.25).all()
+    with pytest.raises(Exception):
+        acc.add_points(np.zeros((3, 3), np.float32), -1.0, (0, 0, 0), 0.1, f)
+    acc.disable_opencl()
+    with pytest.raises(Exception):
+        acc.add_points(np.zeros((1, 3), np.float32), 0.3, (0, 0, 0), 0.1, f)
 
 
 def _random_mac(dims, dx, seed):

@@ -59,3 +59,26 @@ def test_segment_voxel_matches_reference(oracle_lib):
         assert hit == d["hit"][q]
         if hit:
             assert np.array_equal(v, d["voxel"][q])
+
+
+def point_splat_cases():
+    """The general point-splat fixture: inputs and the reference's outputs per case."""
+    d = _load("point_splat.npz")
+    cases = []
+    for t in range(int(d["ncases"])):
+        c = {k[len(f"{t}_"):]: d[k] for k in d.files if k.startswith(f"{t}_")}
+        for k in ("radius", "dx", "threshold"):
+            if k in c:
+                c[k] = float(c[k])
+        cases.append(c)
+    return cases
+
+
+def test_point_splat_matches_reference(oracle_lib):
+    O = oracle_lib
+    for c in point_splat_cases():
+        f, w = O.splat_points(c["points"], c.get("values"), c["radius"], c["offset"], c["dx"], c["field"],
+                              c.get("weight"), c.get("threshold"))
+        assert np.array_equal(f, c["out_field"])
+        if "out_weight" in c:
+            assert np.array_equal(w, c["out_weight"])

@@ -21,6 +21,25 @@ def test_splat(oracle_lib, seed):
         assert np.array_equal(f, rf) and np.array_equal(m.astype(bool), rw > 1e-9)
 
 
+@pytest.mark.parametrize("seed", [7, 8, 9])
+def test_point_splat(oracle_lib, seed):
+    rng = np.random.default_rng(seed)
+    W, H, D = (int(x) for x in rng.integers(5, 12, 3))
+    dx = float(rng.uniform(0.05, 1.0))
+    for rmul in (0.6, 1.0, 1.7, 3.1):
+        n = int(rng.integers(0, 500))
+        pts = rng.uniform(-3 * dx, (max(W, H, D) + 3) * dx, (n, 3)).astype(np.float32)
+        vals = rng.normal(size=n).astype(np.float32) if rmul != 1.0 else None
+        off = rng.uniform(-dx, dx, 3).astype(np.float32)
+        field = rng.uniform(0, 2, (D, H, W)).astype(np.float32)
+        weight = np.zeros_like(field) if rmul > 1.0 else None
+        a = O.splat_points(pts, vals, rmul * dx, off, dx, field, weight)
+        b = O.ref_add_point_values(pts, vals, rmul * dx, off, dx, field, weight)
+        assert np.array_equal(a[0], b[0])
+        if weight is not None:
+            assert np.array_equal(a[1], b[1])
+
+
 @pytest.mark.parametrize("seed", [4, 5])
 def test_pressure_and_extrapolate(oracle_lib, seed):
     sc = scenes.random_box(dims=(12, 10 + seed, 13), seed=seed, solid_blocks=3)
