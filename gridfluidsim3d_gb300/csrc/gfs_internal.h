@@ -101,6 +101,7 @@ struct PressureWs {
     DevMem ctrl;                 // PsCtrl
     DevMem xch;                  // block-boundary exchange words of the wavefronts
     DevMem nbstd, nbsk;          // MIC(0) neighbour bits, padded cell and skewed layouts
+    DevMem blkf;                 // per skew block: 1 if it holds a fluid cell
     size_t nblocks_red = 0;      // blocks of the reduction kernels
     long long allocated_for = -1;
     bool mixed_alloc = false;

@@ -225,7 +225,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_to_skew(Skew K, GridDim c, cons
                                                          const uint16_t *__restrict__ nbits,
                                                          uint8_t *__restrict__ fsk, uint16_t *__restrict__ nbsk,
                                                          double *__restrict__ bsk, double *__restrict__ rsk,
-                                                         double *__restrict__ psk, double *__restrict__ ssk) {
+                                                         double *__restrict__ psk, double *__restrict__ ssk,
+                                                         uint8_t *__restrict__ blkf) {
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < K.size;
          q += (long long)gridDim.x * blockDim.x) {
         int bj, bk, s, jl, kl;
@@ -242,6 +243,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_to_skew(Skew K, GridDim c, cons
         }
         fsk[q] = fl;
         nbsk[q] = nb;
+        if (fl & GFS_PF_FLUID) blkf[bk * K.nbj + bj] = 1;   // same value from every writer
         bsk[q] = bv;
         rsk[q] = bv;
         psk[q] = 0.0;
@@ -283,6 +285,7 @@ struct SweepArgs {
     double scale, dnegscale;
     unsigned long long *xch; // block-boundary exchange words
     const uint16_t *nbits;   // PRECON: skewed MIC(0) neighbour bits
+    const uint8_t *blkf;     // per skew block: 1 if it holds a fluid cell
     unsigned *ticket;        // dispatch ticket
     unsigned *done_ticket;
     double *partials;
@@ -537,12 +540,16 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1) k_sweep(SweepArgs<T> A) {
         bk = K.nbk - 1 - bk;
     }
     const int pbj = bwd ? bj + 1 : bj - 1, pbk = bwd ? bk + 1 : bk - 1;
-    const bool has_pj = pbj >= 0 && pbj < K.nbj, has_pk = pbk >= 0 && pbk < K.nbk;
+    // a block without fluid hands over zeros only (precon is 0 off the fluid set), so it
+    // does no work and its consumers take 0 instead of waiting for it
+    const bool live = A.blkf[bk * K.nbj + bj] != 0;
+    const bool has_pj = pbj >= 0 && pbj < K.nbj && A.blkf[bk * K.nbj + pbj],
+               has_pk = pbk >= 0 && pbk < K.nbk && A.blkf[pbk * K.nbj + bj];
     bool timed_out = false;
 
     const int jl = tid % SBJ, kl = tid / SBJ;
     const int j = bj * SBJ + jl, k = bk * SBK + kl;
-    const bool valid = j < K.ny && k < K.nz;
+    const bool valid = live && j < K.ny && k < K.nz;
     const int xj = bwd ? jl + 1 : jl - 1, xk = bwd ? kl + 1 : kl - 1;
     const bool at_j = bwd ? jl == SBJ - 1 : jl == 0;                // on the upstream j edge
     const bool at_k = bwd ? kl == SBK - 1 : kl == 0;
@@ -615,7 +622,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1) k_sweep(SweepArgs<T> A) {
     Acc2f dot32;         // BWD, FP32: compensated dot(z, r)
     double dot64 = 0.0;  // BWD, FP64
     static_assert(P % PE == 0, "exchange ring must divide the input ring");
-    const int SP = ((S + P - 1) / P) * P;
+    const int SP = live ? ((S + P - 1) / P) * P : 0;
     for (int s0 = 0; s0 < SP; s0 += P) {
 #pragma unroll
         for (int u = 0; u < P; u++) {
@@ -744,12 +751,16 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
     }
     const int pbj = bwd ? bj + 1 : bj - 1, pbk = bwd ? bk + 1 : bk - 1;
     const int cbj = bwd ? bj - 1 : bj + 1, cbk = bwd ? bk - 1 : bk + 1;
-    const bool has_pj = pbj >= 0 && pbj < K.nbj, has_pk = pbk >= 0 && pbk < K.nbk;
-    const bool has_cj = cbj >= 0 && cbj < K.nbj, has_ck = cbk >= 0 && cbk < K.nbk;
+    // blocks without fluid are skipped; their consumers take 0 (see k_sweep)
+    const bool live = A.blkf[bk * K.nbj + bj] != 0;
+    const bool has_pj = pbj >= 0 && pbj < K.nbj && A.blkf[bk * K.nbj + pbj],
+               has_pk = pbk >= 0 && pbk < K.nbk && A.blkf[pbk * K.nbj + bj];
+    const bool has_cj = cbj >= 0 && cbj < K.nbj && A.blkf[bk * K.nbj + cbj],
+               has_ck = cbk >= 0 && cbk < K.nbk && A.blkf[cbk * K.nbj + bj];
     bool timed_out = false;
 
     const int jl = tid % SBJ, kl = tid / SBJ;
-    const bool valid = bj * SBJ + jl < K.ny && bk * SBK + kl < K.nz;
+    const bool valid = live && bj * SBJ + jl < K.ny && bk * SBK + kl < K.nz;
     const int xj = bwd ? jl + 1 : jl - 1, xk = bwd ? kl + 1 : kl - 1;
     const bool at_j = bwd ? jl == SBJ - 1 : jl == 0;
     const bool at_k = bwd ? kl == SBK - 1 : kl == 0;
@@ -783,7 +794,7 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
     // fill the ring with steps 0..P-1
 #pragma unroll
     for (int u = 0; u < P; u++) {
-        if (u < S) {
+        if (u < S && live) {
             cp_async<sizeof(T)>(&ring[0][u][tid], A.in + q0 + u * PS, true);
             cp_async<sizeof(T)>(&ring[1][u][tid], A.precon + q0 + u * PS, true);
             if (bwd) cp_async<sizeof(T)>(&ring[NARR - 1][u][tid], A.rdot + q0 + u * PS, true);
@@ -802,7 +813,7 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
     Acc2f dot32;
     double dot64 = 0.0;
     static_assert(P % PE == 0, "exchange ring must divide the input ring");
-    const int SP = ((S + P - 1) / P) * P;
+    const int SP = live ? ((S + P - 1) / P) * P : 0;
     for (int s0 = 0; s0 < SP; s0 += P) {
 #pragma unroll
         for (int u = 0; u < P; u++) {
@@ -1087,7 +1098,7 @@ static int ensure_ws(Ctx *ctx, PressureWs &ws, const Grids &g, bool mixed) {
         size_t nbl = (size_t)K.nbj * K.nbk;
         size_t np = ws.nblocks_red > nbl ? ws.nblocks_red : nbl;
         if (ws.partials.alloc(np * sizeof(double))) return GFS_ERR_NOMEM;
-        if (ws.ctrl.alloc(sizeof(PsCtrl))) return GFS_ERR_NOMEM;
+        if (ws.ctrl.alloc(sizeof(PsCtrl)) || ws.blkf.alloc(nbl)) return GFS_ERR_NOMEM;
         GFS_CUDA_CHECK(cudaMemsetAsync(ws.ctrl.p, 0, sizeof(PsCtrl), ctx->stream));
         // exchange words: per block and plane XCH_PER_PLANE entries of up to 2 words
         size_t nx_words = nbl * (size_t)K.S * XCH_PER_PLANE * 2;
@@ -1134,6 +1145,7 @@ static int launch_sweep(Ctx *ctx, PressureWs &ws, const T *in, T *out, const T *
     A.dnegscale = -scale;
     A.xch = ws.xch.as<unsigned long long>();
     A.nbits = ws.nbsk.as<uint16_t>();
+    A.blkf = ws.blkf.as<uint8_t>();
     PsCtrl *C = ws.ctrl.as<PsCtrl>();
     A.ticket = &C->sweep_ticket[MODE];
     A.done_ticket = &C->tickets[0];
@@ -1239,9 +1251,10 @@ int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
                                                 ws.b.as<double>(), ws.partials.as<double>(), C);
         dim3 cgrid(grid_blocks(g.c.nx, 128), g.c.ny, g.c.nz);
         k_nbits<<<cgrid, 128, 0, st>>>(g.c, ws.flags.as<uint8_t>(), ws.nbstd.as<uint16_t>());
+        GFS_CUDA_CHECK(cudaMemsetAsync(ws.blkf.p, 0, ws.blkf.bytes, st));
         k_to_skew<<<nb, RED_THREADS, 0, st>>>(K, g.c, ws.flags.as<uint8_t>(), ws.b.as<double>(),
                                                ws.nbstd.as<uint16_t>(), ws.fsk.as<uint8_t>(), ws.nbsk.as<uint16_t>(), ws.bsk.as<double>(), ws.r.as<double>(),
-                                               ws.psk.as<double>(), ws.s.as<double>());
+                                               ws.psk.as<double>(), ws.s.as<double>(), ws.blkf.as<uint8_t>());
     }
     ctx->launches += 3;
     GFS_LAUNCH_CHECK();

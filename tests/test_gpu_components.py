@@ -190,6 +190,35 @@ def test_pressure_plain_matches_oracle(gpu_ctx, oracle_lib, seed, dims):
     assert solver.max_residual < 1e-6 or it_ref == 200
 
 
+def _sparse_fluid(dims, seed):
+    """Material with fluid in separate regions (a slab, a ball, a small box), so that
+    most 16x16 pencil blocks of the pressure solver's layout hold no fluid."""
+    ni, nj, nk = dims
+    mat = scenes.solid_border(dims)
+    k, j, i = np.meshgrid(np.arange(nk), np.arange(nj), np.arange(ni), indexing="ij")
+    fluid = j < 9
+    fluid |= (i - ni / 2) ** 2 + (j - 40) ** 2 + (k - 38) ** 2 < 7.5 ** 2
+    fluid |= (j >= 50) & (j < 55) & (k >= 3) & (k < 9) & (i >= 4) & (i < 12)
+    mat[fluid & (mat != 2)] = 1
+    return mat, _random_mac(dims, 0.1, seed)
+
+
+@pytest.mark.parametrize("precision", [PRECISION_PLAIN, PRECISION_MIXED])
+def test_pressure_blocks_without_fluid(gpu_ctx, oracle_lib, precision):
+    O = oracle_lib
+    dims = (24, 60, 50)
+    mat, f = _sparse_fluid(dims, 11)
+    dt = 1.0 / 30.0
+    want, it_ref, _ = O.pressure_solve(dims, 0.1, 20.0, dt, mat, f.u, f.v, f.w)
+    solver = PressureSolver(gpu_ctx, precision=precision)
+    got = solver.solve(PressureSolverParameters(0.1, 20.0, dt, mat, f))
+    if precision == PRECISION_PLAIN:
+        assert abs(solver.iterations - it_ref) <= 1, (solver.iterations, it_ref)
+        assert np.abs(got - want).max() / np.abs(want).max() < 1e-9
+    res = O.pressure_residual(dims, 0.1, 20.0, dt, mat, f.u, f.v, f.w, got)
+    assert res < 1e-6 or it_ref == 200, res
+
+
 def test_pressure_mixed_reaches_tolerance(gpu_ctx, oracle_lib):
     O = oracle_lib
     sc = scenes.random_box(dims=(30, 22, 26), seed=2)
