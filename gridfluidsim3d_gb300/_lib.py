@@ -88,6 +88,11 @@ _SIGNATURES = {
     "gfs_sim_get_pressure_grid": [_P, _P],
     "gfs_sim_step": [_P, _D, ctypes.POINTER(StepStats)],
     "gfs_sim_step_host": [_P, _D, _P, _P, _P, ctypes.POINTER(_I64), ctypes.POINTER(StepStats)],
+    "gfs_diff_create": [_P, _I, _I64, _D, ctypes.POINTER(_P)],
+    "gfs_diff_destroy": [_P],
+    "gfs_diff_forward": [_P, _P, _P, _P, _P, _P, _P, _P],
+    "gfs_diff_backward": [_P, _P, _P, _P, _P, _P, _P, _P],
+    "gfs_diff_info": [_P, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_I64)],
 }
 
 # entry points declared in include/gfs.h (checked by the CPU test suite)

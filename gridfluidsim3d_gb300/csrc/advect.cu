@@ -16,85 +16,9 @@
 #include <mutex>
 
 #include "gfs_internal.h"
+#include "gfs_interp.cuh"
 
 namespace gfs {
-
-struct AdvArgs {
-    GridDim f[3], c;
-    float inv_dx;      // (float)(1/dx)
-    float bound[3];    // x < dx*n  <=>  x < bound (bound = smallest float >= dx*n)
-    double dx, inv_dx_d;
-    int pow2;
-    float h, f1, f6;   // RK4: (float)(0.5*dt), (float)dt, (float)(dt/6.0f)
-    float a_pic, b_flip;
-};
-
-__device__ __forceinline__ float interp_component(const float *__restrict__ g, const GridDim &f, float X,
-                                                  float Y, float Z) {
-    float fi = floorf(X), fj = floorf(Y), fk = floorf(Z);
-    int i = (int)fi, j = (int)fj, k = (int)fk;
-    float wx[4], wy[4], wz[4];
-    catmull_rom_weights(X - fi, wx);
-    catmull_rom_weights(Y - fj, wy);
-    catmull_rom_weights(Z - fk, wz);
-    const long long sy = f.sx, sz = (long long)f.sx * f.sy;
-    const float *base = g + f.at(i - 1, j - 1, k - 1);
-    float acc = 0.0f;
-#pragma unroll
-    for (int c = 0; c < 4; c++) {
-        float accb = 0.0f;
-#pragma unroll
-        for (int b = 0; b < 4; b++) {
-            const float *row = base + b * sy + c * sz;
-            float r = wx[0] * __ldg(row) + wx[1] * __ldg(row + 1) + wx[2] * __ldg(row + 2) + wx[3] * __ldg(row + 3);
-            accb += wy[b] * r;
-        }
-        acc += wz[c] * accb;
-    }
-    return acc;
-}
-
-// MACVelocityField::evaluateVelocityAtPosition: zero outside [0, n*dx).
-__device__ __forceinline__ float3 eval_velocity(const AdvArgs &A, const float *__restrict__ u,
-                                                const float *__restrict__ v, const float *__restrict__ w,
-                                                float x, float y, float z) {
-    if (!(x >= 0.f && y >= 0.f && z >= 0.f && x < A.bound[0] && y < A.bound[1] && z < A.bound[2]))
-        return make_float3(0.f, 0.f, 0.f);
-    float X, Y, Z;
-    if (A.pow2) {
-        X = x * A.inv_dx;
-        Y = y * A.inv_dx;
-        Z = z * A.inv_dx;
-    } else {
-        X = (float)((double)x * A.inv_dx_d);
-        Y = (float)((double)y * A.inv_dx_d);
-        Z = (float)((double)z * A.inv_dx_d);
-    }
-    // U samples at (i, j+1/2, k+1/2): shift y and z by half a cell, etc.
-    float vx = interp_component(u, A.f[0], X, Y - 0.5f, Z - 0.5f);
-    float vy = interp_component(v, A.f[1], X - 0.5f, Y, Z - 0.5f);
-    float vz = interp_component(w, A.f[2], X - 0.5f, Y - 0.5f, Z);
-    return make_float3(vx, vy, vz);
-}
-
-__device__ __forceinline__ bool finite3(float3 a) { return isfinite(a.x) && isfinite(a.y) && isfinite(a.z); }
-
-__device__ __forceinline__ void pos_cell(const AdvArgs &A, float x, float y, float z, int &i, int &j, int &k) {
-    if (A.pow2) {
-        i = (int)floorf(x * A.inv_dx);
-        j = (int)floorf(y * A.inv_dx);
-        k = (int)floorf(z * A.inv_dx);
-    } else {
-        i = (int)floor((double)x * A.inv_dx_d);
-        j = (int)floor((double)y * A.inv_dx_d);
-        k = (int)floor((double)z * A.inv_dx_d);
-    }
-}
-
-__device__ __forceinline__ bool cell_solid(const AdvArgs &A, const uint8_t *__restrict__ mat, int i, int j, int k) {
-    if (!A.c.in(i, j, k)) return true;   // out of range reads as solid
-    return mat[A.c.at(i, j, k)] == GFS_SOLID;
-}
 
 // Collision::getLineSegmentVoxelIntersection (collision.cpp:303-402)
 __device__ bool segment_voxel(const AdvArgs &A, const uint8_t *__restrict__ mat, float3 p0in, float3 p1in,
@@ -173,17 +97,6 @@ __device__ float3 resolve_collision(const AdvArgs &A, const uint8_t *__restrict_
     return res;
 }
 
-__device__ __forceinline__ float3 axpy3(float3 p, float h, float3 k) {
-    return make_float3(__fadd_rn(p.x, __fmul_rn(h, k.x)), __fadd_rn(p.y, __fmul_rn(h, k.y)),
-                       __fadd_rn(p.z, __fmul_rn(h, k.z)));
-}
-
-// p0 + f6 * (k1 + 2 k2 + 2 k3 + k4), float, left to right (particleadvector.cpp:1051)
-__device__ __forceinline__ float rk4_comb(float p, float f6, float k1, float k2, float k3, float k4) {
-    float sum = __fadd_rn(__fadd_rn(__fadd_rn(k1, __fmul_rn(2.0f, k2)), __fmul_rn(2.0f, k3)), k4);
-    return __fadd_rn(p, __fmul_rn(f6, sum));
-}
-
 __global__ void __launch_bounds__(128) k_g2p_advect(AdvArgs A, float4 *__restrict__ pos, float4 *__restrict__ vel,
                                                     const uint32_t *__restrict__ num, long long nbound,
                                                     const float *__restrict__ mu, const float *__restrict__ mv,
@@ -230,7 +143,7 @@ static float float_ceil_of(double x) {
     return f;
 }
 
-static AdvArgs make_adv(const Grids &g, double dt, double ratio_pic) {
+AdvArgs make_adv(const Grids &g, double dt, double ratio_pic) {
     AdvArgs A;
     for (int d = 0; d < 3; d++) A.f[d] = g.f[d];
     A.c = g.c;

@@ -289,7 +289,7 @@ static int sim_get_particles(Sim *s, float *hp, float *hv, uint32_t *hid, int64_
     return GFS_OK;
 }
 
-static int sim_step(Sim *s, double dt, gfs_step_stats *stats) {
+int sim_step(Sim *s, double dt, gfs_step_stats *stats) {
     Ctx *ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     if (!(dt >= 0.0) || !std::isfinite(dt)) {
@@ -749,6 +749,63 @@ int gfs_pressure_solve(gfs_ctx *ctx, int ni, int nj, int nk, double dx, double d
         GFS_CUDA_CHECK(cudaMemcpyAsync(h_pressure, dout.p, (size_t)F * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         GFS_CUDA_CHECK(cudaStreamSynchronize(c->stream));
     }
+    return GFS_OK;
+}
+
+// ------------------------------------------------ differentiable rollout
+
+struct gfs_diff {
+    gfs::DiffRun *d = nullptr;
+};
+
+int gfs_diff_create(gfs_sim *sim, int nsteps, int64_t n, double dt, gfs_diff **out) {
+    GFS_NONNULL(sim);
+    GFS_NONNULL(out);
+    *out = nullptr;
+    DiffRun *d = nullptr;
+    int rc = diff_create(&sim->s, nsteps, (long long)n, dt, &d);
+    if (rc) return rc;
+    gfs_diff *h = new gfs_diff();
+    h->d = d;
+    *out = h;
+    return GFS_OK;
+}
+
+int gfs_diff_destroy(gfs_diff *d) {
+    if (!d) return GFS_OK;
+    diff_destroy(d->d);
+    delete d;
+    return GFS_OK;
+}
+
+int gfs_diff_forward(gfs_diff *d, const float *d_positions, const float *d_velocities, const float *d_u0,
+                     const float *d_v0, const float *d_w0, float *d_density, float *d_centroids) {
+    GFS_NONNULL(d);
+    GFS_NONNULL(d_positions);
+    if (!d_velocities && (!d_u0 || !d_v0 || !d_w0)) {
+        set_error(GFS_ERR_INVALID, "give initial velocities or the parameter field (u0, v0, w0)");
+        return GFS_ERR_INVALID;
+    }
+    const float *u0[3] = {d_u0, d_v0, d_w0};
+    return diff_forward(d->d, d_positions, d_velocities, u0, d_density, d_centroids);
+}
+
+int gfs_diff_backward(gfs_diff *d, const float *d_grad_density, const float *d_grad_centroids, float *d_grad_u0,
+                      float *d_grad_v0, float *d_grad_w0, float *d_grad_velocities, float *d_grad_positions) {
+    GFS_NONNULL(d);
+    if ((d_grad_u0 || d_grad_v0 || d_grad_w0) && !(d_grad_u0 && d_grad_v0 && d_grad_w0)) {
+        set_error(GFS_ERR_INVALID, "the parameter-field gradient needs all three of u0, v0, w0");
+        return GFS_ERR_INVALID;
+    }
+    float *g[3] = {d_grad_u0, d_grad_v0, d_grad_w0};
+    return diff_backward(d->d, d_grad_density, d_grad_centroids, g, d_grad_velocities, d_grad_positions);
+}
+
+int gfs_diff_info(gfs_diff *d, double *forward_ms, double *backward_ms, int64_t *device_bytes) {
+    GFS_NONNULL(d);
+    long long b = 0;
+    diff_info(d->d, forward_ms, backward_ms, &b);
+    if (device_bytes) *device_bytes = b;
     return GFS_OK;
 }
 

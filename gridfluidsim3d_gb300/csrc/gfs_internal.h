@@ -140,8 +140,21 @@ int exclusive_scan_u32(Ctx *ctx, uint32_t *data_in, uint32_t *data_out, long lon
 size_t scan_temp_elems(long long n);
 
 // ---- splat.cu
-int splat_velocity(Sim *s);           // P2G for U, V, W into sval/smask
+int splat_velocity(Sim *s, float *const wsum[3] = nullptr);   // P2G for U, V, W into sval/smask (+ weight sums)
 int face_fill(Sim *s, double dt);     // a3 + saved copy + body forces
+
+// ---- capi.cu
+int sim_step(Sim *s, double dt, gfs_step_stats *stats);   // one device-resident substep
+
+// ---- adjoint.cu: the differentiable rollout
+struct DiffRun;
+int diff_create(Sim *s, int nsteps, long long n, double dt, DiffRun **out);
+void diff_destroy(DiffRun *d);
+int diff_forward(DiffRun *d, const float *d_pos, const float *d_vel0, const float *const d_u0[3], float *d_density,
+                 float *d_centroids);
+int diff_backward(DiffRun *d, const float *d_rho_bar, const float *d_grad_centroids, float *const d_grad[3],
+                  float *d_grad_vel0, float *d_grad_pos0);
+void diff_info(DiffRun *d, double *fwd_ms, double *bwd_ms, long long *bytes);
 
 // ---- pointsplat.cu
 // General weighted point splat on a W x H x D node grid (device buffers; d_vals
@@ -158,6 +171,11 @@ int extrapolate_field(Sim *s, float *const f[3], int num_layers, bool reset);
 int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
                    float *const mac[3], double density, double dt, int precision, double tol,
                    int max_iters, gfs_step_stats *stats);
+// Solve A x = rhs (padded cell layout, FP64) on the matrix of the last
+// pressure_solve on this workspace, to max|r| < rel_tol * max|rhs|; the
+// solution is left in ws.p.
+int pressure_solve_rhs(Ctx *ctx, PressureWs &ws, const Grids &g, const double *rhs, double density, double dt,
+                       double rel_tol, int max_iters, gfs_step_stats *stats);
 int pressure_apply(Sim *s, double dt);
 int pressure_to_grid(Ctx *ctx, PressureWs &ws, const Grids &g, float *pgrid_unpadded);
 int pressure_gather_compact(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,

@@ -1,0 +1,229 @@
+// gfs_interp.cuh -- MAC-grid sampling shared by the G2P / advection kernels
+// (advect.cu) and their adjoints (adjoint.cu).
+//
+// The sample is MACVelocityField::evaluateVelocityAtPosition
+// (macvelocityfield.cpp:350-559): Catmull-Rom over a 4x4x4 stencil per
+// component (Interpolation::tricubicInterpolate, interpolation.cpp:26-46),
+// evaluated in FP32 in separable form on the padded face grids (the zero halo is
+// the reference's out-of-range value).  The gradient and the transposed
+// (scatter) forms below differentiate exactly that separable sum.
+#pragma once
+
+#include "gfs_internal.h"
+
+namespace gfs {
+
+struct AdvArgs {
+    GridDim f[3], c;
+    float inv_dx;      // (float)(1/dx)
+    float bound[3];    // x < dx*n  <=>  x < bound (bound = smallest float >= dx*n)
+    double dx, inv_dx_d;
+    int pow2;
+    float h, f1, f6;   // RK4: (float)(0.5*dt), (float)dt, (float)(dt/6.0f)
+    float a_pic, b_flip;
+};
+
+__device__ __forceinline__ float interp_component(const float *__restrict__ g, const GridDim &f, float X,
+                                                  float Y, float Z) {
+    float fi = floorf(X), fj = floorf(Y), fk = floorf(Z);
+    int i = (int)fi, j = (int)fj, k = (int)fk;
+    float wx[4], wy[4], wz[4];
+    catmull_rom_weights(X - fi, wx);
+    catmull_rom_weights(Y - fj, wy);
+    catmull_rom_weights(Z - fk, wz);
+    const long long sy = f.sx, sz = (long long)f.sx * f.sy;
+    const float *base = g + f.at(i - 1, j - 1, k - 1);
+    float acc = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        float accb = 0.0f;
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const float *row = base + b * sy + c * sz;
+            float r = wx[0] * __ldg(row) + wx[1] * __ldg(row + 1) + wx[2] * __ldg(row + 2) + wx[3] * __ldg(row + 3);
+            accb += wy[b] * r;
+        }
+        acc += wz[c] * accb;
+    }
+    return acc;
+}
+
+// MACVelocityField::evaluateVelocityAtPosition: zero outside [0, n*dx).
+__device__ __forceinline__ float3 eval_velocity(const AdvArgs &A, const float *__restrict__ u,
+                                                const float *__restrict__ v, const float *__restrict__ w,
+                                                float x, float y, float z) {
+    if (!(x >= 0.f && y >= 0.f && z >= 0.f && x < A.bound[0] && y < A.bound[1] && z < A.bound[2]))
+        return make_float3(0.f, 0.f, 0.f);
+    float X, Y, Z;
+    if (A.pow2) {
+        X = x * A.inv_dx;
+        Y = y * A.inv_dx;
+        Z = z * A.inv_dx;
+    } else {
+        X = (float)((double)x * A.inv_dx_d);
+        Y = (float)((double)y * A.inv_dx_d);
+        Z = (float)((double)z * A.inv_dx_d);
+    }
+    // U samples at (i, j+1/2, k+1/2): shift y and z by half a cell, etc.
+    float vx = interp_component(u, A.f[0], X, Y - 0.5f, Z - 0.5f);
+    float vy = interp_component(v, A.f[1], X - 0.5f, Y, Z - 0.5f);
+    float vz = interp_component(w, A.f[2], X - 0.5f, Y - 0.5f, Z);
+    return make_float3(vx, vy, vz);
+}
+
+__device__ __forceinline__ bool finite3(float3 a) { return isfinite(a.x) && isfinite(a.y) && isfinite(a.z); }
+
+__device__ __forceinline__ void pos_cell(const AdvArgs &A, float x, float y, float z, int &i, int &j, int &k) {
+    if (A.pow2) {
+        i = (int)floorf(x * A.inv_dx);
+        j = (int)floorf(y * A.inv_dx);
+        k = (int)floorf(z * A.inv_dx);
+    } else {
+        i = (int)floor((double)x * A.inv_dx_d);
+        j = (int)floor((double)y * A.inv_dx_d);
+        k = (int)floor((double)z * A.inv_dx_d);
+    }
+}
+
+__device__ __forceinline__ bool cell_solid(const AdvArgs &A, const uint8_t *__restrict__ mat, int i, int j, int k) {
+    if (!A.c.in(i, j, k)) return true;   // out of range reads as solid
+    return mat[A.c.at(i, j, k)] == GFS_SOLID;
+}
+
+
+__device__ __forceinline__ float3 axpy3(float3 p, float h, float3 k) {
+    return make_float3(__fadd_rn(p.x, __fmul_rn(h, k.x)), __fadd_rn(p.y, __fmul_rn(h, k.y)),
+                       __fadd_rn(p.z, __fmul_rn(h, k.z)));
+}
+
+// p0 + f6 * (k1 + 2 k2 + 2 k3 + k4), float, left to right (particleadvector.cpp:1051)
+__device__ __forceinline__ float rk4_comb(float p, float f6, float k1, float k2, float k3, float k4) {
+    float sum = __fadd_rn(__fadd_rn(__fadd_rn(k1, __fmul_rn(2.0f, k2)), __fmul_rn(2.0f, k3)), k4);
+    return __fadd_rn(p, __fmul_rn(f6, sum));
+}
+
+
+AdvArgs make_adv(const Grids &g, double dt, double ratio_pic);
+
+// d/dx of the Catmull-Rom basis weights of catmull_rom_weights
+__device__ __forceinline__ void catmull_rom_dweights(float x, float d[4]) {
+    float x2 = x * x;
+    d[0] = 0.5f * (-1.0f + 4.0f * x - 3.0f * x2);
+    d[1] = 0.5f * (-10.0f * x + 9.0f * x2);
+    d[2] = 0.5f * (1.0f + 8.0f * x - 9.0f * x2);
+    d[3] = 0.5f * (3.0f * x2 - 2.0f * x);
+}
+
+// Sample and gradient (in index units) of one component at index-space (X, Y, Z).
+__device__ __forceinline__ float interp_component_grad(const float *__restrict__ g, const GridDim &f, float X,
+                                                       float Y, float Z, float grad[3]) {
+    float fi = floorf(X), fj = floorf(Y), fk = floorf(Z);
+    int i = (int)fi, j = (int)fj, k = (int)fk;
+    float wx[4], wy[4], wz[4], dx_[4], dy_[4], dz_[4];
+    catmull_rom_weights(X - fi, wx);
+    catmull_rom_weights(Y - fj, wy);
+    catmull_rom_weights(Z - fk, wz);
+    catmull_rom_dweights(X - fi, dx_);
+    catmull_rom_dweights(Y - fj, dy_);
+    catmull_rom_dweights(Z - fk, dz_);
+    const long long sy = f.sx, sz = (long long)f.sx * f.sy;
+    const float *base = g + f.at(i - 1, j - 1, k - 1);
+    float acc = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        float ab = 0.f, abx = 0.f, aby = 0.f;
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const float *row = base + b * sy + c * sz;
+            float v0 = __ldg(row), v1 = __ldg(row + 1), v2 = __ldg(row + 2), v3 = __ldg(row + 3);
+            float r = wx[0] * v0 + wx[1] * v1 + wx[2] * v2 + wx[3] * v3;
+            float rx = dx_[0] * v0 + dx_[1] * v1 + dx_[2] * v2 + dx_[3] * v3;
+            ab += wy[b] * r;
+            abx += wy[b] * rx;
+            aby += dy_[b] * r;
+        }
+        acc += wz[c] * ab;
+        gx += wz[c] * abx;
+        gy += wz[c] * aby;
+        gz += dz_[c] * ab;
+    }
+    grad[0] = gx;
+    grad[1] = gy;
+    grad[2] = gz;
+    return acc;
+}
+
+// Transpose of interp_component: g[node] += weight(node) * c (atomically).
+__device__ __forceinline__ void scatter_component(float *__restrict__ g, const GridDim &f, float X, float Y, float Z,
+                                                  float c) {
+    if (c == 0.0f) return;
+    float fi = floorf(X), fj = floorf(Y), fk = floorf(Z);
+    int i = (int)fi, j = (int)fj, k = (int)fk;
+    float wx[4], wy[4], wz[4];
+    catmull_rom_weights(X - fi, wx);
+    catmull_rom_weights(Y - fj, wy);
+    catmull_rom_weights(Z - fk, wz);
+    const long long sy = f.sx, sz = (long long)f.sx * f.sy;
+    float *base = g + f.at(i - 1, j - 1, k - 1);
+#pragma unroll
+    for (int cc = 0; cc < 4; cc++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            float wbc = wz[cc] * wy[b] * c;
+            float *row = base + b * sy + cc * sz;
+#pragma unroll
+            for (int a = 0; a < 4; a++) atomicAdd(row + a, wx[a] * wbc);
+        }
+}
+
+// Index-space coordinates of a world position (as eval_velocity forms them).
+__device__ __forceinline__ void to_index(const AdvArgs &A, float x, float y, float z, float &X, float &Y, float &Z) {
+    if (A.pow2) {
+        X = x * A.inv_dx;
+        Y = y * A.inv_dx;
+        Z = z * A.inv_dx;
+    } else {
+        X = (float)((double)x * A.inv_dx_d);
+        Y = (float)((double)y * A.inv_dx_d);
+        Z = (float)((double)z * A.inv_dx_d);
+    }
+}
+
+__device__ __forceinline__ bool inside(const AdvArgs &A, float x, float y, float z) {
+    return x >= 0.f && y >= 0.f && z >= 0.f && x < A.bound[0] && y < A.bound[1] && z < A.bound[2];
+}
+
+// Velocity and its Jacobian J[r][c] = d v_r / d x_c (world units) at a position.
+__device__ __forceinline__ float3 eval_velocity_jac(const AdvArgs &A, const float *__restrict__ u,
+                                                    const float *__restrict__ v, const float *__restrict__ w,
+                                                    float x, float y, float z, float J[3][3]) {
+#pragma unroll
+    for (int r = 0; r < 3; r++) J[r][0] = J[r][1] = J[r][2] = 0.f;
+    if (!inside(A, x, y, z)) return make_float3(0.f, 0.f, 0.f);
+    float X, Y, Z;
+    to_index(A, x, y, z, X, Y, Z);
+    const float s = (float)A.inv_dx_d;
+    float vx = interp_component_grad(u, A.f[0], X, Y - 0.5f, Z - 0.5f, J[0]);
+    float vy = interp_component_grad(v, A.f[1], X - 0.5f, Y, Z - 0.5f, J[1]);
+    float vz = interp_component_grad(w, A.f[2], X - 0.5f, Y - 0.5f, Z, J[2]);
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        J[r][0] *= s;
+        J[r][1] *= s;
+        J[r][2] *= s;
+    }
+    return make_float3(vx, vy, vz);
+}
+
+// Transpose of eval_velocity: adds c (a velocity adjoint) into the face grids.
+__device__ __forceinline__ void scatter_velocity(const AdvArgs &A, float *__restrict__ u, float *__restrict__ v,
+                                                 float *__restrict__ w, float x, float y, float z, float3 c) {
+    if (!inside(A, x, y, z)) return;
+    float X, Y, Z;
+    to_index(A, x, y, z, X, Y, Z);
+    scatter_component(u, A.f[0], X, Y - 0.5f, Z - 0.5f, c.x);
+    scatter_component(v, A.f[1], X - 0.5f, Y, Z - 0.5f, c.y);
+    scatter_component(w, A.f[2], X - 0.5f, Y - 0.5f, Z, c.z);
+}
+
+}  // namespace gfs

@@ -1384,6 +1384,122 @@ int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
     return GFS_OK;
 }
 
+// ------------------------------------------- solve with a given right-hand side
+
+// b = rhs on the fluid cells of the current flags; control block reset as
+// k_ps_setup does, with the stopping threshold relative to max|rhs|.
+__global__ void __launch_bounds__(RED_THREADS) k_set_rhs(GridDim c, const uint8_t *__restrict__ flags,
+                                                         const double *__restrict__ rhs, double *__restrict__ b,
+                                                         double *__restrict__ partials, PsCtrl *ctrl,
+                                                         double rel_tol) {
+    double mx = 0.0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < c.size;
+         e += (long long)gridDim.x * blockDim.x) {
+        double v = (flags[e] & GFS_PF_FLUID) ? rhs[e] : 0.0;
+        b[e] = v;
+        mx = fmax(mx, fabs(v));
+    }
+    double part = block_reduce<1>(mx);
+    double res;
+    if (finish_reduce<1>(part, partials, &ctrl->tickets[0], gridDim.x, &res) && threadIdx.x == 0) {
+        ctrl->maxb = res;
+        ctrl->maxr = res;
+        ctrl->maxr64 = res;
+        ctrl->tol = rel_tol * res;
+        ctrl->iter = 0;
+        ctrl->converged = 0;
+        ctrl->total_inner = 0;
+        ctrl->refinements = 0;
+        ctrl->sigma = 0.0;
+        ctrl->alpha = 0.0;
+        ctrl->beta = 0.0;
+        ctrl->done = res > 0.0 ? 0 : 1;
+    }
+}
+
+int pressure_solve_rhs(Ctx *ctx, PressureWs &ws, const Grids &g, const double *rhs, double density, double dt,
+                       double rel_tol, int max_iters, gfs_step_stats *stats) {
+    if (ws.allocated_for != g.c.size) {
+        set_error(GFS_ERR_STATE, "pressure_solve_rhs needs a pressure solve on this grid first");
+        return GFS_ERR_STATE;
+    }
+    cudaStream_t st = ctx->stream;
+    const double dx = g.dx;
+    const double scale = dt / (density * dx * dx);
+    PsCtrl *C = ws.ctrl.as<PsCtrl>();
+    const Skew K = make_skew(g.c);
+    {
+        PsCtrl h;
+        memset(&h, 0, sizeof(h));
+        GFS_CUDA_CHECK(cudaMemcpyAsync(&h, C, sizeof(PsCtrl), cudaMemcpyDeviceToHost, st));
+        GFS_CUDA_CHECK(cudaStreamSynchronize(st));
+        h.max_iters = max_iters;
+        h.err = 0;
+        if (h.epoch == 0) h.epoch = 1;
+        GFS_CUDA_CHECK(cudaMemcpyAsync(C, &h, sizeof(PsCtrl), cudaMemcpyHostToDevice, st));
+    }
+    unsigned nb = (unsigned)ws.nblocks_red;
+    {
+        ProfScope prof(ctx, KC_PS_SETUP);
+        k_set_rhs<<<nb, RED_THREADS, 0, st>>>(g.c, ws.flags.as<uint8_t>(), rhs, ws.b.as<double>(),
+                                               ws.partials.as<double>(), C, rel_tol);
+        GFS_CUDA_CHECK(cudaMemsetAsync(ws.blkf.p, 0, ws.blkf.bytes, st));
+        k_to_skew<<<nb, RED_THREADS, 0, st>>>(K, g.c, ws.flags.as<uint8_t>(), ws.b.as<double>(),
+                                               ws.nbstd.as<uint16_t>(), ws.fsk.as<uint8_t>(), ws.nbsk.as<uint16_t>(),
+                                               ws.bsk.as<double>(), ws.r.as<double>(), ws.psk.as<double>(),
+                                               ws.s.as<double>(), ws.blkf.as<uint8_t>());
+    }
+    ctx->launches += 2;
+    GFS_LAUNCH_CHECK();
+    PsCtrl h;
+    int rc = read_ctrl(ctx, ws, &h);
+    if (rc) return rc;
+    int sweeps = 0;
+    if (!h.done) {
+        double *p = ws.psk.as<double>(), *r = ws.r.as<double>(), *z = ws.z.as<double>(), *s = ws.s.as<double>(),
+               *As = ws.As.as<double>(), *q = ws.q.as<double>(), *pc = ws.precon.as<double>();
+        rc = launch_sweep<double, SW_PRECON>(ctx, ws, nullptr, pc, nullptr, nullptr, nullptr, scale, 0);
+        if (rc) return rc;
+        rc = launch_sweep<double, SW_FWD>(ctx, ws, r, q, pc, nullptr, nullptr, scale, 0);
+        if (rc) return rc;
+        rc = launch_sweep<double, SW_BWD>(ctx, ws, q, z, pc, r, nullptr, scale, 1);
+        if (rc) return rc;
+        VecArgs<double> V = vec_args<double>(ws, scale, 0);
+        {
+            ProfScope prof(ctx, KC_UPDATE_S);
+            k_update_s<double><<<nb, RED_THREADS, 0, st>>>(V, z, s);
+        }
+        ctx->launches++;
+        for (;;) {
+            for (int it = 0; it < CG_CHUNK; it++) {
+                rc = cg_iteration<double>(ctx, ws, scale, 0, p, r, z, s, As, q, pc);
+                if (rc) return rc;
+            }
+            rc = read_ctrl(ctx, ws, &h);
+            if (rc) return rc;
+            if (h.done) break;
+        }
+        sweeps = 1 + h.iter;
+    }
+    {
+        dim3 grid(grid_blocks(g.c.nx, 128), g.c.ny, g.c.nz);
+        k_from_skew<<<grid, 128, 0, st>>>(K, g.c, ws.flags.as<uint8_t>(), ws.psk.as<double>(), ws.p.as<double>());
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+    }
+    if (h.err) {
+        set_error(GFS_ERR_TIMEOUT, "a wavefront wait of the pressure solve timed out");
+        return GFS_ERR_TIMEOUT;
+    }
+    if (stats) {
+        stats->cg_iterations = h.iter;
+        stats->cg_max_residual = h.maxr;
+        stats->refinements = 0;
+        stats->sweeps = sweeps;
+    }
+    return GFS_OK;
+}
+
 // ------------------------------------------------------ apply pressure
 
 struct ApplyArgs {

@@ -50,7 +50,9 @@ __global__ void __launch_bounds__(128) k_splat_gather(SplatArgs A, const float4 
                                                       const uint32_t *__restrict__ offset,
                                                       float *__restrict__ uval, uint8_t *__restrict__ umask,
                                                       float *__restrict__ vval, uint8_t *__restrict__ vmask,
-                                                      float *__restrict__ wval, uint8_t *__restrict__ wmask) {
+                                                      float *__restrict__ wval, uint8_t *__restrict__ wmask,
+                                                      float *__restrict__ usum, float *__restrict__ vsum,
+                                                      float *__restrict__ wsum) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y * blockDim.y + threadIdx.y;
     int k = blockIdx.z * blockDim.z + threadIdx.z;
@@ -107,20 +109,24 @@ __global__ void __launch_bounds__(128) k_splat_gather(SplatArgs A, const float4 
         }
     }
     // ScalarField::applyWeightField (scalarfield.cpp:90-106) and the 1e-9 mask
+    // (weight sums on request: the adjoint of the division needs them)
     if (vu) {
         long long f = A.f[0].at(i, j, k);
         uval[f] = wu > 0.f ? su / wu : su;
         umask[f] = wu > A.set_thresh;
+        if (usum) usum[f] = wu;
     }
     if (vv) {
         long long f = A.f[1].at(i, j, k);
         vval[f] = wv > 0.f ? sv / wv : sv;
         vmask[f] = wv > A.set_thresh;
+        if (vsum) vsum[f] = wv;
     }
     if (vw) {
         long long f = A.f[2].at(i, j, k);
         wval[f] = ww > 0.f ? sw / ww : sw;
         wmask[f] = ww > A.set_thresh;
+        if (wsum) wsum[f] = ww;
     }
 }
 
@@ -136,7 +142,7 @@ static float float_floor_of(double x) {
     return f;
 }
 
-int splat_velocity(Sim *s) {
+int splat_velocity(Sim *s, float *const wsum[3]) {
     Ctx *ctx = s->ctx;
     ProfScope prof(ctx, KC_SPLAT);
     SplatArgs A;
@@ -152,7 +158,8 @@ int splat_velocity(Sim *s) {
     k_splat_gather<<<grid, block, 0, ctx->stream>>>(
         A, s->pos.as<float4>(), s->vel.as<float4>(), s->offset.as<uint32_t>(), s->sval[0].as<float>(),
         s->smask[0].as<uint8_t>(), s->sval[1].as<float>(), s->smask[1].as<uint8_t>(),
-        s->sval[2].as<float>(), s->smask[2].as<uint8_t>());
+        s->sval[2].as<float>(), s->smask[2].as<uint8_t>(), wsum ? wsum[0] : nullptr, wsum ? wsum[1] : nullptr,
+        wsum ? wsum[2] : nullptr);
     ctx->launches++;
     GFS_LAUNCH_CHECK();
     return GFS_OK;

@@ -149,5 +149,25 @@ def random_box(dims=(16, 12, 14), dx: float = 0.1, seed: int = 0, ppc: int = 8,
     return _finish("random_box", dims, dx, mat, pos, vel, seed)
 
 
+def diff_cube(n: int = 32, dx: float = 0.25, cube: int = 12, ppc: int = 8, seed: int = 4):
+    """Differentiable-control scene (small): an n^3 grid with solid walls, a cube of
+    `cube`^3 fluid cells at the centre with `ppc` particles per cell uniform in each
+    cell, a parameter MAC field U(-1, 1), and a target cell density: a Gaussian
+    blob of sigma 3 cells, 6 cells in +x from the cube centre, with the total of
+    the initial density (computed by the caller's density operator)."""
+    dims = (n, n, n)
+    rng = np.random.default_rng(seed)
+    mat = solid_border(dims)
+    lo = (n - cube) // 2
+    fluid = np.zeros(dims[::-1], bool)
+    fluid[lo:lo + cube, lo:lo + cube, lo:lo + cube] = True
+    pos = seed_particles(fluid, dx, ppc, rng)
+    u0 = [rng.uniform(-1.0, 1.0, size=shape).astype(np.float32)
+          for shape in ((n, n, n + 1), (n, n + 1, n), (n + 1, n, n))]
+    center = (n / 2 + 6.0, n / 2, n / 2)
+    return dict(dims=dims, dx=dx, dt=1.0 / 30.0, steps=20, mat=mat, pos=pos, u0=u0, target_center=center,
+                target_sigma=3.0)
+
+
 SCENES = {"ball_drop": ball_drop, "dam_break": dam_break, "slab_spheres": slab_spheres,
           "random_box": random_box}

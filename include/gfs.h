@@ -231,6 +231,42 @@ int gfs_sim_step(gfs_sim *sim, double dt, gfs_step_stats *stats);
 int gfs_sim_step_host(gfs_sim *sim, double dt, float *h_positions, float *h_velocities,
                       uint32_t *h_ids, int64_t *n, gfs_step_stats *stats);
 
+/* ------------------------------------------------ differentiable rollout */
+
+/* A differentiable rollout of `nsteps` substeps of length dt over n particles
+   on a simulation's grid, material and parameters (no counterpart in the
+   reference; the forward model is the substep of gfs_sim_step).  Particles
+   start at d_positions (n x 3) with the velocities d_velocities (n x 3) or, if
+   that is NULL, velocities sampled (Catmull-Rom, as G2P samples) from the
+   parameter MAC field d_u0 / d_v0 / d_w0.  Outputs (each may be NULL): the
+   cell-centred particle density after the last substep (ni*nj*nk floats, splat
+   kernel 1 - 4/9 s^3 + 17/9 s^2 - 22/9 s of radius 1.5 dx at cell centres) and
+   the particle centroid at the start of every substep and at the end
+   ((nsteps + 1) x 3 floats).  The forward keeps every substep's particle state on
+   the device; the backward recomputes each substep's grids from it and runs the
+   adjoint of every stage with the substep's discrete structure (fluid cells,
+   splat set masks, fill and extrapolation structure) held fixed; the pressure
+   adjoint is a second MIC(0)-PCG solve with the same matrix.  Collisions and
+   the per-cell cap are not differentiated: a forward in which particles are
+   removed fails with GFS_ERR_STATE.  All pointers are DEVICE pointers on the
+   simulation's GPU; face fields are unpadded, x fastest; per-particle arrays
+   are in the input order.  The calls synchronise the context's stream. */
+typedef struct gfs_diff gfs_diff;
+int gfs_diff_create(gfs_sim *sim, int nsteps, int64_t n, double dt, gfs_diff **out);
+int gfs_diff_destroy(gfs_diff *d);
+int gfs_diff_forward(gfs_diff *d, const float *d_positions, const float *d_velocities, const float *d_u0,
+                     const float *d_v0, const float *d_w0, float *d_density, float *d_centroids);
+/* Gradients of a loss from its gradients with respect to the forward's outputs
+   (d_grad_density, d_grad_centroids; NULL = not part of the loss).  Outputs
+   (each may be NULL): the parameter field's gradient (when the velocities were
+   sampled from it), the initial velocities' gradient, and the starting
+   positions' gradient with the initial velocities held fixed. */
+int gfs_diff_backward(gfs_diff *d, const float *d_grad_density, const float *d_grad_centroids,
+                      float *d_grad_u0, float *d_grad_v0, float *d_grad_w0, float *d_grad_velocities,
+                      float *d_grad_positions);
+/* Device time of the last forward / backward and the rollout's own device bytes. */
+int gfs_diff_info(gfs_diff *d, double *forward_ms, double *backward_ms, int64_t *device_bytes);
+
 /* Number of kernel launches the library has issued on this context (for
    accounting in benchmarks). */
 int gfs_ctx_launch_count(gfs_ctx *ctx, int64_t *count);
