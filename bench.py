@@ -21,6 +21,9 @@ roofline   the dominant kernel class of the timed region: algorithmic bytes per
 cpu_baseline  the oracle (C restatement of the reference's CPU path, single
            thread like the reference) timed on a bounded sample of this workload
            and scaled to one substep.
+adjoint    fwd+adjoint ms/substep and peak HBM of the two differentiable
+           configurations (32^3 cube, 20 substeps, MAC-field parameters; 128^3
+           dam break, 60 substeps, per-particle velocities, Adam steps).
 
 --impl reference times that CPU path alone and prints its own line.
 --gpus N (under torchrun): N independent replicas (the exact MIC(0)
@@ -297,6 +300,94 @@ def profile_read(ctx):
     return out
 
 
+def adjoint_bench(ctx, iters=2, warmup=1):
+    """fwd+adjoint ms/step of the two differentiable configurations.
+
+    small: 32^3, dx 0.25, 12^3 cube, 8 ppc, 20 substeps; parameters the initial
+    MAC field U(-1,1); loss the L2 distance of the final cell density to a
+    Gaussian blob (sigma 3 cells, 6 cells in +x).
+    scale: the 128^3 dam break (8 ppc), 60 substeps, gravity (0,-25,0);
+    parameters the per-particle initial velocities; loss the L2 distance of the
+    centroid trajectory to a target moving 4 cells in +x; Adam steps on the
+    initial velocities.
+    ms/step = (forward + backward device time of one iteration) / substeps,
+    CUDA events around the library calls; peak HBM = device total - lowest free
+    memory seen during the iterations (device-wide)."""
+    import torch
+    from gridfluidsim3d_gb300 import PRECISION_MIXED, FluidSimulation, scenes
+    from gridfluidsim3d_gb300.autograd import FlipRollout
+    dev = torch.device("cuda", torch.cuda.current_device())
+    out = {}
+
+    def run(name, sim, steps, dt, n, make_loss, params, opt):
+        roll = FlipRollout(sim, steps, dt, n)
+        low = torch.cuda.mem_get_info(dev)[0]
+        fwd, bwd, losses = [], [], []
+        for it in range(warmup + iters):
+            opt.zero_grad()
+            loss = make_loss(roll)
+            loss.backward()
+            opt.step()
+            torch.cuda.synchronize(dev)
+            low = min(low, torch.cuda.mem_get_info(dev)[0])
+            f, b, nbytes = roll.info()
+            if it >= warmup:
+                fwd.append(f)
+                bwd.append(b)
+            losses.append(float(loss.detach()))
+        total = torch.cuda.mem_get_info(dev)[1]
+        roll.close()
+        f, b = statistics.mean(fwd), statistics.mean(bwd)
+        out[name] = {"substeps": steps, "particles": n, "fwd_ms": round(f, 2), "bwd_ms": round(b, 2),
+                     "fwd_adjoint_ms_per_step": round((f + b) / steps, 3), "bwd_over_fwd": round(b / f, 3),
+                     "rollout_device_bytes": int(nbytes), "peak_hbm_bytes": int(total - low),
+                     "loss": losses}
+
+    # small: parameter field, density loss
+    sc = scenes.diff_cube()
+    sim = FluidSimulation(*sc["dims"], sc["dx"], max_particles=len(sc["pos"]), ctx=ctx)
+    sim.reset_body_force()
+    sim.precision = PRECISION_MIXED
+    sim.set_material_grid(sc["mat"])
+    xs = torch.tensor(sc["pos"], device=dev)
+    u = [torch.tensor(a, device=dev, requires_grad=True) for a in sc["u0"]]
+    dims, dx = sc["dims"], sc["dx"]
+    ni, nj, nk = dims
+    k, j, i = np.meshgrid(np.arange(nk), np.arange(nj), np.arange(ni), indexing="ij")
+    c = sc["target_center"]
+    blob = np.exp(-((i + 0.5 - c[0]) ** 2 + (j + 0.5 - c[1]) ** 2 + (k + 0.5 - c[2]) ** 2) / (2 * 3.0 ** 2))
+    # total density of a 12^3 cube at 8 ppc: about the particle count times the mean kernel mass
+    tgt = torch.tensor(blob / blob.sum(), device=dev, dtype=torch.float32)
+
+    def loss_small(roll):
+        rho, _ = roll(xs, u0=u[0], v0=u[1], w0=u[2])
+        return ((rho - tgt * rho.detach().sum()) ** 2).sum()
+
+    run("32^3 cube, 20 substeps, MAC-field parameters", sim, sc["steps"], sc["dt"], len(sc["pos"]), loss_small, u,
+        torch.optim.Adam(u, lr=0.05))
+    sim.close()
+    # scale: per-particle velocities, centroid trajectory
+    db = scenes.dam_break(128)
+    sim = FluidSimulation(*db.dims, db.dx, max_particles=db.num_particles, ctx=ctx)
+    sim.precision = PRECISION_MIXED
+    sim.set_material_grid(db.mat)
+    steps = int(db.meta["substeps"])
+    xs5 = torch.tensor(db.pos, device=dev)
+    v = torch.zeros((db.num_particles, 3), device=dev, requires_grad=True)
+    c0 = xs5.mean(0)
+    goal = c0[None, :] + torch.linspace(0, 1, steps + 1, device=dev)[:, None] * torch.tensor(
+        [4 * db.dx, 0.0, 0.0], device=dev)
+
+    def loss_scale(roll):
+        _, cen = roll(xs5, velocities=v)
+        return ((cen - goal) ** 2).sum()
+
+    run("128^3 dam break, 60 substeps, per-particle velocities", sim, steps, db.dt, db.num_particles, loss_scale, [v],
+        torch.optim.Adam([v], lr=0.05))
+    sim.close()
+    return out
+
+
 def main(args):
     if args.impl == "reference":
         return reference_main(args)
@@ -364,6 +455,10 @@ def main(args):
     ctx.synchronize()
     te = reduce_max(time.perf_counter() - t0, world)
 
+    adjoint = None
+    if r == 0 and world == 1 and not args.no_adjoint and set(forms) == {"plain", "mixed"}:
+        sim.close()
+        adjoint = adjoint_bench(ctx)
     if r == 0 and set(forms) != {"plain", "mixed"}:
         # partial run (profiling): report the timed forms only
         print(json.dumps({k: {"ms_per_step": v["t"] / args.steps * 1e3, "gpu_launches": int(v["launches"])}
@@ -439,7 +534,7 @@ def main(args):
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": clocks,
-            "adjoint": None,
+            "adjoint": adjoint,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -457,6 +552,7 @@ def parse():
     ap.add_argument("--forms", default="plain,mixed",
                     help="pressure forms to time (a partial set prints a short line; for profiling)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-rollout leg")
     ap.add_argument("--ref-cg-iterations", type=int, default=200,
                     help="CG iterations the reference arm scales its per-iteration cost to")
     a = ap.parse_args()

@@ -5,14 +5,15 @@
 // velocities sampled from a parameter MAC field (Catmull-Rom, as G2P samples),
 // run `nsteps` substeps of the device-resident core (capi.cu sim_step), and the
 // output is the cell-centred particle density (splat kernel of radius 1.5 dx).
-// The particle state at the start of every substep is kept in HBM.
+// The particle state at the start of every substep and every substep's pressure
+// are kept in HBM.
 //
 // Backward (gfs_diff_backward), substep by substep in reverse, with the
 // discrete structure (fluid cells, splat set masks, fill contributors,
 // extrapolation layers) of the substep held fixed:
 //   1. recompute the substep's grids from its checkpoint (classify, splat with
-//      weight sums, fill, layers, saved extrapolation, pressure, apply,
-//      extrapolation);
+//      weight sums, fill, layers, saved extrapolation, pressure set-up, apply of
+//      the checkpointed pressure, extrapolation);
 //   2. k_adj_g2p: per particle, the adjoint of the FLIP update and of RK4
 //      through the Jacobians of the Catmull-Rom samples; the sample adjoints
 //      scatter into the MAC / saved adjoint face grids (atomics);
@@ -28,8 +29,10 @@
 //   7. k_adj_p2g: per particle, the adjoint of u = sum w v / sum w (a gather
 //      over the faces within dx of the particle, quotient rule for the weights).
 // Adjoints travel per particle id, since every substep re-sorts the particles.
-// Collisions and the per-cell cap are not differentiated: the forward reports
-// an error if any particle is removed.
+// Collisions and removals (particles left in solid cells, the per-cell cap) are
+// not differentiated: a particle removed during a substep has zero adjoint from
+// then on, and its earlier state is differentiated through the substeps it
+// took part in.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -533,12 +536,15 @@ __global__ void k_diff_centroid_out(const double *__restrict__ c, int count, dou
     if (q < count) out[q] = (float)(c[q] * inv_n);
 }
 
-// x_bar += g_c / n for every particle (the centroid's adjoint at one substep)
-__global__ void k_adj_centroid(float4 *__restrict__ ax, long long n, const float *__restrict__ gc, float inv_n) {
+// x_bar += g_c / n for every particle present at one substep boundary (the
+// centroid's adjoint there); pos lists those particles, ax is indexed by id
+__global__ void k_adj_centroid(const float4 *__restrict__ pos, float4 *__restrict__ ax, long long n,
+                               const float *__restrict__ gc, float inv_n) {
     long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (q >= n) return;
-    float4 X = ax[q];
-    ax[q] = make_float4(X.x + gc[0] * inv_n, X.y + gc[1] * inv_n, X.z + gc[2] * inv_n, 0.f);
+    uint32_t id = pid(pos[q]);
+    float4 X = ax[id];
+    ax[id] = make_float4(X.x + gc[0] * inv_n, X.y + gc[1] * inv_n, X.z + gc[2] * inv_n, 0.f);
 }
 
 // id-ordered xyz of a by-id float4 array
@@ -578,7 +584,9 @@ struct DiffRun {
     DevMem g0[3], g1[3], g2[3], wsum[3], cnt[3], par[3];   // padded face grids
     DevMem pbar;                     // padded cells, double
     DevMem cen;                      // (nsteps + 1) x 3 position sums, double
+    DevMem ckp;                      // nsteps x padded-cell pressure of every substep (double)
     bool sampled = true;             // initial velocities sampled from the parameter field
+    std::vector<long long> count;    // particles at the start of every substep (and at the end)
     double fwd_ms = 0.0, bwd_ms = 0.0;
     size_t peak_bytes = 0;
 };
@@ -609,6 +617,7 @@ static int diff_alloc(DiffRun *d) {
     }
     if (d->pbar.alloc((size_t)g.c.size * sizeof(double))) return GFS_ERR_NOMEM;
     if (d->cen.alloc((size_t)(d->nsteps + 1) * 3 * sizeof(double))) return GFS_ERR_NOMEM;
+    if (d->ckp.alloc((size_t)d->nsteps * g.c.size * sizeof(double))) return GFS_ERR_NOMEM;
     GFS_CUDA_CHECK(cudaMemsetAsync(d->pbar.p, 0, d->pbar.bytes, s->ctx->stream));
     return GFS_OK;
 }
@@ -623,14 +632,15 @@ static int recompute(DiffRun *d, int step, float *const wsum[3]) {
     Sim *s = d->s;
     Ctx *ctx = s->ctx;
     cudaStream_t st = ctx->stream;
-    GFS_CUDA_CHECK(cudaMemcpyAsync(s->pos.p, ck_pos(d, step), d->n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
-    GFS_CUDA_CHECK(cudaMemcpyAsync(s->vel.p, ck_vel(d, step), d->n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
-    uint32_t num[4] = {(uint32_t)d->n, 0, 0, 0};
+    const long long m = d->count[step];
+    GFS_CUDA_CHECK(cudaMemcpyAsync(s->pos.p, ck_pos(d, step), m * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    GFS_CUDA_CHECK(cudaMemcpyAsync(s->vel.p, ck_vel(d, step), m * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    uint32_t num[4] = {(uint32_t)m, 0, 0, 0};
     GFS_CUDA_CHECK(cudaMemcpyAsync(s->num.p, num, sizeof(num), cudaMemcpyHostToDevice, st));
-    s->n_bound = d->n;
+    s->n_bound = m;
     int rc;
     if ((rc = sort_particles(s, false))) return rc;   // already in (cell, id) order: rebuilds the cell lists
-    if ((long long)s->n_bound != d->n) {
+    if ((long long)s->n_bound != m) {
         set_error(GFS_ERR_STATE, "checkpoint %d lost particles on re-sort", step);
         return GFS_ERR_STATE;
     }
@@ -643,10 +653,10 @@ static int recompute(DiffRun *d, int step, float *const wsum[3]) {
     float *saved[3] = {s->saved[0].as<float>(), s->saved[1].as<float>(), s->saved[2].as<float>()};
     if ((rc = extrapolate_field(s, saved, layers, false))) return rc;
     float *mac[3] = {s->mac[0].as<float>(), s->mac[1].as<float>(), s->mac[2].as<float>()};
-    gfs_step_stats local{};
-    rc = pressure_solve(ctx, s->ps, s->g, s->mat.as<uint8_t>(), mac, s->params.density, d->dt, s->params.precision,
-                        s->params.tol, s->params.max_cg_iterations, &local);
-    if (rc) return rc;
+    // the system's set-up for the adjoint solve; the pressure itself is the forward's
+    if ((rc = pressure_setup(ctx, s->ps, s->g, s->mat.as<uint8_t>(), mac))) return rc;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(s->ps.p.p, d->ckp.as<double>() + (size_t)step * s->g.c.size,
+                                   (size_t)s->g.c.size * sizeof(double), cudaMemcpyDeviceToDevice, st));
     if ((rc = pressure_apply(s, d->dt))) return rc;
     return extrapolate_field(s, mac, layers, false);
 }
@@ -700,7 +710,8 @@ void diff_info(DiffRun *d, double *fwd_ms, double *bwd_ms, long long *bytes) {
     if (fwd_ms) *fwd_ms = d->fwd_ms;
     if (bwd_ms) *bwd_ms = d->bwd_ms;
     if (bytes) {
-        size_t b = d->ck.bytes + d->ax.bytes + d->av.bytes + d->bx.bytes + d->bv.bytes + d->pbar.bytes;
+        size_t b = d->ck.bytes + d->ckp.bytes + d->cen.bytes + d->ax.bytes + d->av.bytes + d->bx.bytes +
+                   d->bv.bytes + d->pbar.bytes;
         for (int q = 0; q < 3; q++)
             b += d->g0[q].bytes + d->g1[q].bytes + d->g2[q].bytes + d->wsum[q].bytes + d->cnt[q].bytes +
                  d->par[q].bytes;
@@ -744,19 +755,26 @@ int diff_forward(DiffRun *d, const float *d_pos, const float *d_vel0, const floa
     }
     ctx->launches++;
     GFS_LAUNCH_CHECK();
+    if ((long long)s->n_bound != d->n) {
+        set_error(GFS_ERR_INVALID, "%lld of the %lld starting particles lie in solid cells or over the per-cell cap",
+                  d->n - (long long)s->n_bound, d->n);
+        return GFS_ERR_INVALID;
+    }
+    d->count.assign(d->nsteps + 1, 0);
+    long long m = d->n;
     for (int step = 0; step < d->nsteps; step++) {
-        GFS_CUDA_CHECK(cudaMemcpyAsync(ck_pos(d, step), s->pos.p, d->n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
-        GFS_CUDA_CHECK(cudaMemcpyAsync(ck_vel(d, step), s->vel.p, d->n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+        d->count[step] = m;
+        GFS_CUDA_CHECK(cudaMemcpyAsync(ck_pos(d, step), s->pos.p, m * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+        GFS_CUDA_CHECK(cudaMemcpyAsync(ck_vel(d, step), s->vel.p, m * sizeof(float4), cudaMemcpyDeviceToDevice, st));
         gfs_step_stats stats{};
         if ((rc = sim_step(s, d->dt, &stats))) return rc;
-        if (stats.num_particles != d->n) {
-            set_error(GFS_ERR_STATE, "substep %d removed particles (collision or per-cell cap); the rollout is not "
-                                     "differentiable there", step);
-            return GFS_ERR_STATE;
-        }
+        GFS_CUDA_CHECK(cudaMemcpyAsync(d->ckp.as<double>() + (size_t)step * g.c.size, s->ps.p.p,
+                                       (size_t)g.c.size * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        m = stats.num_particles;
     }
-    GFS_CUDA_CHECK(cudaMemcpyAsync(ck_pos(d, d->nsteps), s->pos.p, d->n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
-    GFS_CUDA_CHECK(cudaMemcpyAsync(ck_vel(d, d->nsteps), s->vel.p, d->n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    d->count[d->nsteps] = m;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(ck_pos(d, d->nsteps), s->pos.p, m * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    GFS_CUDA_CHECK(cudaMemcpyAsync(ck_vel(d, d->nsteps), s->vel.p, m * sizeof(float4), cudaMemcpyDeviceToDevice, st));
     const double R = DIFF_DENSITY_RADIUS * g.dx;
     dim3 cgrid(grid_blocks(g.c.nx, 128), g.c.ny, g.c.nz);
     if (d_density) {
@@ -766,11 +784,12 @@ int diff_forward(DiffRun *d, const float *d_pos, const float *d_vel0, const floa
     }
     if (d_centroids) {
         GFS_CUDA_CHECK(cudaMemsetAsync(d->cen.p, 0, d->cen.bytes, st));
-        for (int step = 0; step <= d->nsteps; step++)
-            k_diff_centroid<<<64, 256, 0, st>>>(ck_pos(d, step), d->n, d->cen.as<double>() + 3 * step);
-        k_diff_centroid_out<<<grid_blocks(3 * (d->nsteps + 1), 128), 128, 0, st>>>(
-            d->cen.as<double>(), 3 * (d->nsteps + 1), 1.0 / (double)d->n, d_centroids);
-        ctx->launches += d->nsteps + 2;
+        for (int step = 0; step <= d->nsteps; step++) {
+            k_diff_centroid<<<64, 256, 0, st>>>(ck_pos(d, step), d->count[step], d->cen.as<double>() + 3 * step);
+            k_diff_centroid_out<<<1, 32, 0, st>>>(d->cen.as<double>() + 3 * step, 3, 1.0 / (double)d->count[step],
+                                                  d_centroids + 3 * step);
+        }
+        ctx->launches += 2 * (d->nsteps + 1);
     }
     GFS_LAUNCH_CHECK();
     cudaEventRecord(e1, st);
@@ -800,20 +819,20 @@ int diff_backward(DiffRun *d, const float *d_rho_bar, const float *d_grad_centro
     cudaEventRecord(e0, st);
     const int T = 128;
     const double R = DIFF_DENSITY_RADIUS * g.dx;
-    // density adjoint at the final positions (or zero adjoints)
+    // density adjoint at the final positions (ids removed earlier keep zero adjoints)
+    GFS_CUDA_CHECK(cudaMemsetAsync(d->ax.p, 0, d->ax.bytes, st));
+    GFS_CUDA_CHECK(cudaMemsetAsync(d->av.p, 0, d->av.bytes, st));
+    const long long mN = d->count[d->nsteps];
     if (d_rho_bar) {
-        k_adj_density<<<grid_blocks(d->n, T), T, 0, st>>>(g.c, g.dx, ck_pos(d, d->nsteps), d->n, d_rho_bar,
-                                                          (float)(1.0 / (R * R)), d->ax.as<float4>(),
-                                                          d->av.as<float4>());
+        k_adj_density<<<grid_blocks(mN, T), T, 0, st>>>(g.c, g.dx, ck_pos(d, d->nsteps), mN, d_rho_bar,
+                                                        (float)(1.0 / (R * R)), d->ax.as<float4>(),
+                                                        d->av.as<float4>());
         ctx->launches++;
-    } else {
-        GFS_CUDA_CHECK(cudaMemsetAsync(d->ax.p, 0, d->ax.bytes, st));
-        GFS_CUDA_CHECK(cudaMemsetAsync(d->av.p, 0, d->av.bytes, st));
     }
-    const float inv_n = (float)(1.0 / (double)d->n);
     if (d_grad_centroids) {
-        k_adj_centroid<<<grid_blocks(d->n, T), T, 0, st>>>(d->ax.as<float4>(), d->n,
-                                                           d_grad_centroids + 3 * d->nsteps, inv_n);
+        k_adj_centroid<<<grid_blocks(mN, T), T, 0, st>>>(ck_pos(d, d->nsteps), d->ax.as<float4>(), mN,
+                                                         d_grad_centroids + 3 * d->nsteps,
+                                                         (float)(1.0 / (double)mN));
         ctx->launches++;
     }
     GFS_LAUNCH_CHECK();
@@ -843,11 +862,15 @@ int diff_backward(DiffRun *d, const float *d_rho_bar, const float *d_grad_centro
     float *wp[3];
     for (int step = d->nsteps - 1; step >= 0; step--) {
         if ((rc = recompute(d, step, fptr(d->wsum, wp)))) return rc;
-        // 2. G2P / RK4: g0 = MAC adjoint, g1 = saved adjoint
+        const long long m = d->count[step];
+        // 2. G2P / RK4: g0 = MAC adjoint, g1 = saved adjoint; (bx, bv) by id, zero for
+        // ids not present in this substep
         if ((rc = zero_faces(ctx, d->g0))) return rc;
         if ((rc = zero_faces(ctx, d->g1))) return rc;
-        k_adj_g2p<<<grid_blocks(d->n, T), T, 0, st>>>(
-            A, s->pos.as<float4>(), s->vel.as<float4>(), d->n, s->mac[0].as<float>(), s->mac[1].as<float>(),
+        GFS_CUDA_CHECK(cudaMemsetAsync(d->bx.p, 0, d->bx.bytes, st));
+        GFS_CUDA_CHECK(cudaMemsetAsync(d->bv.p, 0, d->bv.bytes, st));
+        k_adj_g2p<<<grid_blocks(m, T), T, 0, st>>>(
+            A, s->pos.as<float4>(), s->vel.as<float4>(), m, s->mac[0].as<float>(), s->mac[1].as<float>(),
             s->mac[2].as<float>(), s->saved[0].as<float>(), s->saved[1].as<float>(), s->saved[2].as<float>(),
             d->ax.as<float4>(), d->av.as<float4>(), d->bx.as<float4>(), d->bv.as<float4>(), d->g0[0].as<float>(),
             d->g0[1].as<float>(), d->g0[2].as<float>(), d->g1[0].as<float>(), d->g1[1].as<float>(),
@@ -864,7 +887,7 @@ int diff_backward(DiffRun *d, const float *d_rho_bar, const float *d_grad_centro
         ctx->launches++;
         GFS_LAUNCH_CHECK();
         gfs_step_stats ps{};
-        if ((rc = pressure_solve_rhs(ctx, s->ps, g, d->pbar.as<double>(), s->params.density, d->dt, 1e-9, 2000, &ps)))
+        if ((rc = pressure_solve_rhs(ctx, s->ps, g, d->pbar.as<double>(), s->params.density, d->dt, 1e-7, 2000, &ps)))
             return rc;
         k_adj_div<<<face_grid(g.c), face_block(), 0, st>>>(P, s->mat.as<uint8_t>(), s->ps.p.as<double>(),
                                                           d->g0[0].as<float>(), d->g0[1].as<float>(),
@@ -890,8 +913,8 @@ int diff_backward(DiffRun *d, const float *d_rho_bar, const float *d_grad_centro
         ctx->launches += 2;
         GFS_LAUNCH_CHECK();
         // 7. P2G into (bx, bv), then they become the adjoints of this substep's start
-        k_adj_p2g<<<grid_blocks(d->n, T), T, 0, st>>>(
-            SA, s->pos.as<float4>(), s->vel.as<float4>(), d->n, s->sval[0].as<float>(), s->sval[1].as<float>(),
+        k_adj_p2g<<<grid_blocks(m, T), T, 0, st>>>(
+            SA, s->pos.as<float4>(), s->vel.as<float4>(), m, s->sval[0].as<float>(), s->sval[1].as<float>(),
             s->sval[2].as<float>(), s->smask[0].as<uint8_t>(), s->smask[1].as<uint8_t>(), s->smask[2].as<uint8_t>(),
             d->wsum[0].as<float>(), d->wsum[1].as<float>(), d->wsum[2].as<float>(), d->g2[0].as<float>(),
             d->g2[1].as<float>(), d->g2[2].as<float>(), d->bx.as<float4>(), d->bv.as<float4>());
@@ -900,8 +923,8 @@ int diff_backward(DiffRun *d, const float *d_rho_bar, const float *d_grad_centro
         std::swap(d->ax.p, d->bx.p);
         std::swap(d->av.p, d->bv.p);
         if (d_grad_centroids) {   // the centroid at the start of this substep
-            k_adj_centroid<<<grid_blocks(d->n, T), T, 0, st>>>(d->ax.as<float4>(), d->n,
-                                                               d_grad_centroids + 3 * step, inv_n);
+            k_adj_centroid<<<grid_blocks(m, T), T, 0, st>>>(ck_pos(d, step), d->ax.as<float4>(), m,
+                                                            d_grad_centroids + 3 * step, (float)(1.0 / (double)m));
             ctx->launches++;
         }
     }

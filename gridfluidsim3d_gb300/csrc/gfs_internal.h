@@ -171,6 +171,8 @@ int extrapolate_field(Sim *s, float *const f[3], int num_layers, bool reset);
 int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
                    float *const mac[3], double density, double dt, int precision, double tol,
                    int max_iters, gfs_step_stats *stats);
+// The system's flags, b and neighbour bits only (no solve).
+int pressure_setup(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat, float *const mac[3]);
 // Solve A x = rhs (padded cell layout, FP64) on the matrix of the last
 // pressure_solve on this workspace, to max|r| < rel_tol * max|rhs|; the
 // solution is left in ws.p.

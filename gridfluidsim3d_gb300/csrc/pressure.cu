@@ -1384,6 +1384,36 @@ int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
     return GFS_OK;
 }
 
+// ------------------------------------------------ setup without a solve
+
+// Flags, b and neighbour bits of the system for (mat, mac) -- what
+// pressure_solve does before its first sweep -- so that pressure_solve_rhs
+// can solve with the same matrix and a caller can supply the pressure itself.
+int pressure_setup(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat, float *const mac[3]) {
+    int rc = ensure_ws(ctx, ws, g, false);
+    if (rc) return rc;
+    cudaStream_t st = ctx->stream;
+    const double dx = g.dx;
+    PsCtrl *C = ws.ctrl.as<PsCtrl>();
+    SetupArgs SA;
+    SA.c = g.c;
+    SA.fu = g.f[0];
+    SA.fv = g.f[1];
+    SA.fw = g.f[2];
+    SA.fscale = 1.0f / (float)dx;
+    SA.scale_div = (double)(1.0f / (float)dx);
+    SA.tol = 1e-6;
+    unsigned nb = (unsigned)ws.nblocks_red;
+    ProfScope prof(ctx, KC_PS_SETUP);
+    k_ps_setup<<<nb, RED_THREADS, 0, st>>>(SA, mat, mac[0], mac[1], mac[2], ws.flags.as<uint8_t>(), ws.b.as<double>(),
+                                            ws.partials.as<double>(), C);
+    dim3 cgrid(grid_blocks(g.c.nx, 128), g.c.ny, g.c.nz);
+    k_nbits<<<cgrid, 128, 0, st>>>(g.c, ws.flags.as<uint8_t>(), ws.nbstd.as<uint16_t>());
+    ctx->launches += 2;
+    GFS_LAUNCH_CHECK();
+    return GFS_OK;
+}
+
 // ------------------------------------------- solve with a given right-hand side
 
 // b = rhs on the fluid cells of the current flags; control block reset as
