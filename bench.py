@@ -21,6 +21,9 @@ roofline   the dominant kernel class of the timed region: algorithmic bytes per
 cpu_baseline  the oracle (C restatement of the reference's CPU path, single
            thread like the reference) timed on a bounded sample of this workload
            and scaled to one substep.
+accuracy_vs_fp64  per timed substep (re-run untimed): max|p - p_ref| / max|p_ref|
+           against an FP64 PCG solve of the same system to 1e-12, and the FP64
+           residual max|b - A p| of the step's pressure, for both forms.
 adjoint    fwd+adjoint ms/substep and peak HBM of the two differentiable
            configurations (32^3 cube, 20 substeps, MAC-field parameters; 128^3
            dam break, 60 substeps, per-particle velocities, Adam steps).
@@ -306,10 +309,11 @@ def adjoint_bench(ctx, iters=2, warmup=1):
     small: 32^3, dx 0.25, 12^3 cube, 8 ppc, 20 substeps; parameters the initial
     MAC field U(-1,1); loss the L2 distance of the final cell density to a
     Gaussian blob (sigma 3 cells, 6 cells in +x).
-    scale: the 128^3 dam break (8 ppc), 60 substeps, gravity (0,-25,0);
-    parameters the per-particle initial velocities; loss the L2 distance of the
-    centroid trajectory to a target moving 4 cells in +x; Adam steps on the
-    initial velocities.
+    scale: the 128^3 dam-break particle layout (8 ppc, at rest, no gravity: with
+    gravity the rollout is dominated by wall collisions and is not a
+    differentiable map), 60 substeps; parameters the per-particle initial
+    velocities; loss the L2 distance of the centroid trajectory to a target
+    moving 4 cells in +x; Adam steps on the initial velocities.
     ms/step = (forward + backward device time of one iteration) / substeps,
     CUDA events around the library calls; peak HBM = device total - lowest free
     memory seen during the iterations (device-wide)."""
@@ -370,6 +374,7 @@ def adjoint_bench(ctx, iters=2, warmup=1):
     db = scenes.dam_break(128)
     sim = FluidSimulation(*db.dims, db.dx, max_particles=db.num_particles, ctx=ctx)
     sim.precision = PRECISION_MIXED
+    sim.reset_body_force()
     sim.set_material_grid(db.mat)
     steps = int(db.meta["substeps"])
     xs5 = torch.tensor(db.pos, device=dev)
@@ -382,7 +387,7 @@ def adjoint_bench(ctx, iters=2, warmup=1):
         _, cen = roll(xs5, velocities=v)
         return ((cen - goal) ** 2).sum()
 
-    run("128^3 dam break, 60 substeps, per-particle velocities", sim, steps, db.dt, db.num_particles, loss_scale, [v],
+    run("128^3 dam-break layout, 60 substeps, per-particle velocities", sim, steps, db.dt, db.num_particles, loss_scale, [v],
         torch.optim.Adam([v], lr=0.05))
     sim.close()
     return out
@@ -429,6 +434,24 @@ def main(args):
         prof = profile_read(ctx)
         results[name] = dict(t=reduce_max(t, world), stats=stats, launches=launches, prof=prof,
                              clocks=clk.summary())
+
+    # accuracy against FP64 (untimed): the same substeps again, each followed by an
+    # FP64 MIC(0)-PCG solve of its pressure system to 1e-12 relative
+    accuracy = {}
+    if not args.no_check:
+        for name, prec in (("plain", PRECISION_PLAIN), ("mixed", PRECISION_MIXED)):
+            if name not in forms:
+                continue
+            sim.precision = prec
+            reset(sim, sc)
+            run_steps(sim, sc, args.warmup, dt)
+            errs, res = [], []
+            for _ in range(args.steps):
+                sim.update(dt)
+                chk = sim.pressure_check(dt)
+                errs.append(chk["rel_error"])
+                res.append(chk["fp64_residual"])
+            accuracy[name] = {"pressure_rel_error_vs_fp64": errs, "fp64_residual": res}
 
     # end-to-end through the host-buffer entry point (mixed form)
     sim.precision = PRECISION_MIXED
@@ -522,6 +545,7 @@ def main(args):
                       "cg_iterations": [s["cg_iterations"] for s in plain["stats"]],
                       "max_residual": [s["cg_max_residual"] for s in plain["stats"]],
                       "ms_per_stage": pbreak},
+            "accuracy_vs_fp64": accuracy,
             "mixed": {"cg_iterations": [s["cg_iterations"] for s in st],
                       "refinements": [s["refinements"] for s in st],
                       "max_residual": [s["cg_max_residual"] for s in st],
@@ -553,6 +577,7 @@ def parse():
                     help="pressure forms to time (a partial set prints a short line; for profiling)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-rollout leg")
+    ap.add_argument("--no-check", action="store_true", help="skip the per-step FP64 pressure check")
     ap.add_argument("--ref-cg-iterations", type=int, default=200,
                     help="CG iterations the reference arm scales its per-iteration cost to")
     a = ap.parse_args()

@@ -88,6 +88,7 @@ _SIGNATURES = {
     "gfs_sim_get_pressure_grid": [_P, _P],
     "gfs_sim_step": [_P, _D, ctypes.POINTER(StepStats)],
     "gfs_sim_step_host": [_P, _D, _P, _P, _P, ctypes.POINTER(_I64), ctypes.POINTER(StepStats)],
+    "gfs_sim_pressure_check": [_P, _D, _D, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_I)],
     "gfs_diff_create": [_P, _I, _I64, _D, ctypes.POINTER(_P)],
     "gfs_diff_destroy": [_P],
     "gfs_diff_forward": [_P, _P, _P, _P, _P, _P, _P, _P],

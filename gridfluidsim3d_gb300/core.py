@@ -443,6 +443,14 @@ class FluidSimulation:
         self.current_frame += 1
         return self.last_stats
 
+    def pressure_check(self, dt, rel_tol=1e-12) -> dict:
+        """Error of the last step's pressure against an FP64 solve of the same system
+        to rel_tol: {"fp64_residual": max|b - A p|, "rel_error": max|p - p_ref| / max|p_ref|}."""
+        r, e, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        _lib.lib().gfs_sim_pressure_check(self._h, float(dt), float(rel_tol), ctypes.byref(r), ctypes.byref(e),
+                                          ctypes.byref(it))
+        return {"fp64_residual": r.value, "rel_error": e.value, "ref_iterations": it.value}
+
     def update_host(self, dt, positions, velocities, ids):
         """The same substep on host-resident particle arrays (copied in and out):
         arrays are updated in place; returns (count, stats)."""

@@ -29,10 +29,11 @@
 //   7. k_adj_p2g: per particle, the adjoint of u = sum w v / sum w (a gather
 //      over the faces within dx of the particle, quotient rule for the weights).
 // Adjoints travel per particle id, since every substep re-sorts the particles.
-// Collisions and removals (particles left in solid cells, the per-cell cap) are
-// not differentiated: a particle removed during a substep has zero adjoint from
-// then on, and its earlier state is differentiated through the substeps it
-// took part in.
+// A solid collision is differentiated through its placement (the end point
+// pulled back before the entry plane of the first solid voxel, with the voxel
+// and the plane held fixed).  Removals (particles left in solid cells, the
+// per-cell cap) are not differentiated: a particle removed during a substep has
+// zero adjoint from then on.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -170,7 +171,8 @@ __global__ void __launch_bounds__(128) k_adj_g2p(AdvArgs A, const float4 *__rest
                                                  float4 *__restrict__ ax_out, float4 *__restrict__ av_out,
                                                  float *__restrict__ gmu, float *__restrict__ gmv,
                                                  float *__restrict__ gmw, float *__restrict__ gsu,
-                                                 float *__restrict__ gsv, float *__restrict__ gsw) {
+                                                 float *__restrict__ gsv, float *__restrict__ gsw,
+                                                 const uint8_t *__restrict__ mat) {
     long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (q >= n) return;
     const float4 P = pos[q];
@@ -187,13 +189,52 @@ __global__ void __launch_bounds__(128) k_adj_g2p(AdvArgs A, const float4 *__rest
     float3 y3 = axpy3(x, A.h, k2);
     float3 k3 = eval_velocity_jac(A, mu, mv, mw, y3.x, y3.y, y3.z, J3);
     float3 y4 = axpy3(x, A.f1, k3);
-    eval_velocity_jac(A, mu, mv, mw, y4.x, y4.y, y4.z, J4);
+    float3 k4 = eval_velocity_jac(A, mu, mv, mw, y4.x, y4.y, y4.z, J4);
+    // the step's end point and its collision, exactly as k_g2p_advect forms them
+    float3 p1 = make_float3(rk4_comb(x.x, A.f6, k1.x, k2.x, k3.x, k4.x), rk4_comb(x.y, A.f6, k1.y, k2.y, k3.y, k4.y),
+                            rk4_comb(x.z, A.f6, k1.z, k2.z, k3.z, k4.z));
+    float3 xb_rk = xb, xb_direct = make_float3(0.f, 0.f, 0.f);
+    {
+        int ci, cj, ck;
+        pos_cell(A, p1.x, p1.y, p1.z, ci, cj, ck);
+        if (!(isfinite(p1.x) && isfinite(p1.y) && isfinite(p1.z)) || cell_solid(A, mat, ci, cj, ck)) {
+            CollisionHit hit;
+            resolve_collision(A, mat, x, p1, &hit);
+            if (!hit.moved) {
+                // the particle kept its position: p1' = p0
+                xb_rk = make_float3(0.f, 0.f, 0.f);
+                xb_direct = xb;
+            } else {
+                // p1' = p0 + ((b - p0_a) / u_a - back) u, u = (p1 - p0) / |p1 - p0|, entry plane x_a = b
+                // (resolve_collision, collision.cpp:404-449), differentiated in p0 and p1
+                const float q[3] = {p1.x - x.x, p1.y - x.y, p1.z - x.z};
+                const float L = sqrtf(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+                const float u[3] = {q[0] / L, q[1] / L, q[2] / L};
+                const float g[3] = {xb.x, xb.y, xb.z};
+                const float p0a[3] = {x.x, x.y, x.z};
+                const int a = hit.axis;
+                const float ua = u[a];
+                const float back = (float)(0.05 * A.dx);
+                const float da = hit.plane - p0a[a];
+                const float sv = da / ua - back;
+                const float ug = u[0] * g[0] + u[1] * g[1] + u[2] * g[2];
+                float qb[3], dr[3];
+                for (int c = 0; c < 3; c++) {
+                    float ea = c == a ? 1.f : 0.f;
+                    qb[c] = -da / (ua * ua * L) * (ea - ua * u[c]) * ug + (sv / L) * (g[c] - u[c] * ug);
+                    dr[c] = g[c] - ea * ug / ua - qb[c];
+                }
+                xb_rk = make_float3(qb[0], qb[1], qb[2]);
+                xb_direct = make_float3(dr[0], dr[1], dr[2]);
+            }
+        }
+    }
     // FLIP: v' = a_pic a + b_flip (v + a - s)
     const float3 abar = f3scale(vb, A.a_pic + A.b_flip);
     const float3 sbar = f3scale(vb, -A.b_flip);
     // RK4: x' = x + f6 (k1 + 2 k2 + 2 k3 + k4)
-    float3 xbar = xb;
-    float3 kb1 = f3scale(xb, A.f6), kb2 = f3scale(xb, 2.0f * A.f6), kb3 = kb2, kb4 = kb1;
+    float3 xbar = f3add(xb_rk, xb_direct);
+    float3 kb1 = f3scale(xb_rk, A.f6), kb2 = f3scale(xb_rk, 2.0f * A.f6), kb3 = kb2, kb4 = kb1;
     {   // stage 4: k4 = u(y4), y4 = x + f1 k3
         float3 yb = mtv(J4, kb4);
         scatter_velocity(A, gmu, gmv, gmw, y4.x, y4.y, y4.z, kb4);
@@ -874,7 +915,7 @@ int diff_backward(DiffRun *d, const float *d_rho_bar, const float *d_grad_centro
             s->mac[2].as<float>(), s->saved[0].as<float>(), s->saved[1].as<float>(), s->saved[2].as<float>(),
             d->ax.as<float4>(), d->av.as<float4>(), d->bx.as<float4>(), d->bv.as<float4>(), d->g0[0].as<float>(),
             d->g0[1].as<float>(), d->g0[2].as<float>(), d->g1[0].as<float>(), d->g1[1].as<float>(),
-            d->g1[2].as<float>());
+            d->g1[2].as<float>(), s->mat.as<uint8_t>());
         ctx->launches++;
         GFS_LAUNCH_CHECK();
         // 3. extrapolations

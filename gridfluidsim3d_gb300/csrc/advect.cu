@@ -20,83 +20,6 @@
 
 namespace gfs {
 
-// Collision::getLineSegmentVoxelIntersection (collision.cpp:303-402)
-__device__ bool segment_voxel(const AdvArgs &A, const uint8_t *__restrict__ mat, float3 p0in, float3 p1in,
-                              int &vi, int &vj, int &vk) {
-    float s = (float)(1.0 / A.dx);
-    float p0x = __fmul_rn(p0in.x, s), p0y = __fmul_rn(p0in.y, s), p0z = __fmul_rn(p0in.z, s);
-    float p1x = __fmul_rn(p1in.x, s), p1y = __fmul_rn(p1in.y, s), p1z = __fmul_rn(p1in.z, s);
-    int gx0 = (int)floorf(p0x), gy0 = (int)floorf(p0y), gz0 = (int)floorf(p0z);
-    int gx1 = (int)floorf(p1x), gy1 = (int)floorf(p1y), gz1 = (int)floorf(p1z);
-    int sx = gx1 > gx0 ? 1 : gx1 < gx0 ? -1 : 0;
-    int sy = gy1 > gy0 ? 1 : gy1 < gy0 ? -1 : 0;
-    int sz = gz1 > gz0 ? 1 : gz1 < gz0 ? -1 : 0;
-    int gx = gx0, gy = gy0, gz = gz0;
-    double gxp = gx0 + (gx1 > gx0 ? 1 : 0), gyp = gy0 + (gy1 > gy0 ? 1 : 0), gzp = gz0 + (gz1 > gz0 ? 1 : 0);
-    double vx = p1x == p0x ? 1.0 : (double)__fsub_rn(p1x, p0x);
-    double vy = p1y == p0y ? 1.0 : (double)__fsub_rn(p1y, p0y);
-    double vz = p1z == p0z ? 1.0 : (double)__fsub_rn(p1z, p0z);
-    double vxvy = vx * vy, vxvz = vx * vz, vyvz = vy * vz;
-    double errx = (gxp - (double)p0x) * vyvz, erry = (gyp - (double)p0y) * vxvz, errz = (gzp - (double)p0z) * vxvy;
-    double derrx = sx * vyvz, derry = sy * vxvz, derrz = sz * vxvy;
-    int limit = abs(gx1 - gx0) + abs(gy1 - gy0) + abs(gz1 - gz0) + 3;
-    for (int it = 0; it < limit; it++) {
-        if (A.c.in(gx, gy, gz) && mat[A.c.at(gx, gy, gz)] == GFS_SOLID) {
-            vi = gx; vj = gy; vk = gz;
-            return true;
-        }
-        if (gx == gx1 && gy == gy1 && gz == gz1) break;
-        double xr = fabs(errx), yr = fabs(erry), zr = fabs(errz);
-        if (sx != 0 && (sy == 0 || xr < yr) && (sz == 0 || xr < zr)) { gx += sx; errx += derrx; }
-        else if (sy != 0 && (sz == 0 || yr < zr)) { gy += sy; erry += derry; }
-        else if (sz != 0) { gz += sz; errz += derrz; }
-    }
-    return false;
-}
-
-// FluidSimulation::_resolveParticleSolidCellCollision (fluidsimulation.cpp:3145-3179)
-// with Collision::rayIntersectsAABB (collision.cpp:404-449, including its use of
-// dir.x to guard dir.z).
-__device__ float3 resolve_collision(const AdvArgs &A, const uint8_t *__restrict__ mat, float3 p0, float3 p1) {
-    int vi, vj, vk;
-    if (!segment_voxel(A, mat, p0, p1, vi, vj, vk)) return p0;
-    float dxr = __fsub_rn(p1.x, p0.x), dyr = __fsub_rn(p1.y, p0.y), dzr = __fsub_rn(p1.z, p0.z);
-    float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dxr, dxr), __fmul_rn(dyr, dyr)), __fmul_rn(dzr, dzr)));
-    float linv = (float)(1.0 / (double)len);
-    float3 rn = make_float3(__fmul_rn(dxr, linv), __fmul_rn(dyr, linv), __fmul_rn(dzr, linv));
-    float bmin[3], bmax[3];
-    int vv[3] = {vi, vj, vk};
-    for (int q = 0; q < 3; q++) {
-        bmin[q] = (float)((double)(float)vv[q] * A.dx);
-        bmax[q] = __fadd_rn(bmin[q], (float)A.dx);
-    }
-    float dir[3] = {rn.x, rn.y, rn.z};
-    const double eps = 1e-10;
-    if (fabs((double)dir[0]) < eps) dir[0] = dir[0] < 0 ? (float)-eps : (float)eps;
-    if (fabs((double)dir[1]) < eps) dir[1] = dir[1] < 0 ? (float)-eps : (float)eps;
-    if (fabs((double)dir[0]) < eps) dir[2] = dir[2] < 0 ? (float)-eps : (float)eps;
-    float inv[3] = {(float)(1.0 / (double)dir[0]), (float)(1.0 / (double)dir[1]), (float)(1.0 / (double)dir[2])};
-    float p0a[3] = {p0.x, p0.y, p0.z};
-    double tmin = 0, tmax = 0;
-    for (int q = 0; q < 3; q++) {
-        double t1 = (double)__fmul_rn(__fsub_rn(bmin[q], p0a[q]), inv[q]);
-        double t2 = (double)__fmul_rn(__fsub_rn(bmax[q], p0a[q]), inv[q]);
-        if (q == 0) { tmin = fmin(t1, t2); tmax = fmax(t1, t2); }
-        else { tmin = fmax(tmin, fmin(t1, t2)); tmax = fmin(tmax, fmax(t1, t2)); }
-    }
-    if (!(tmax > fmax(tmin, 0.0))) return p0;
-    float ft = (float)tmin;
-    float cp[3];
-    for (int q = 0; q < 3; q++) cp[q] = __fadd_rn(p0a[q], __fmul_rn(ft, dir[q]));
-    float back = (float)(0.05 * A.dx);
-    float3 res = make_float3(__fsub_rn(cp[0], __fmul_rn(back, rn.x)), __fsub_rn(cp[1], __fmul_rn(back, rn.y)),
-                             __fsub_rn(cp[2], __fmul_rn(back, rn.z)));
-    int ri, rj, rk;
-    pos_cell(A, res.x, res.y, res.z, ri, rj, rk);
-    if (cell_solid(A, mat, ri, rj, rk)) return p0;
-    return res;
-}
-
 __global__ void __launch_bounds__(128) k_g2p_advect(AdvArgs A, float4 *__restrict__ pos, float4 *__restrict__ vel,
                                                     const uint32_t *__restrict__ num, long long nbound,
                                                     const float *__restrict__ mu, const float *__restrict__ mv,

@@ -752,6 +752,18 @@ int gfs_pressure_solve(gfs_ctx *ctx, int ni, int nj, int nk, double dx, double d
     return GFS_OK;
 }
 
+int gfs_sim_pressure_check(gfs_sim *sim, double dt, double rel_tol, double *fp64_residual, double *rel_error,
+                           int *ref_iterations) {
+    GFS_NONNULL(sim);
+    Sim *s = &sim->s;
+    if (!(dt > 0.0) || !(rel_tol > 0.0)) {
+        set_error(GFS_ERR_INVALID, "dt and rel_tol must be > 0");
+        return GFS_ERR_INVALID;
+    }
+    return pressure_check(s->ctx, s->ps, s->g, s->params.density, dt, rel_tol, fp64_residual, rel_error,
+                          ref_iterations);
+}
+
 // ------------------------------------------------ differentiable rollout
 
 struct gfs_diff {

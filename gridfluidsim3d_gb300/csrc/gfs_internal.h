@@ -171,6 +171,11 @@ int extrapolate_field(Sim *s, float *const f[3], int num_layers, bool reset);
 int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
                    float *const mac[3], double density, double dt, int precision, double tol,
                    int max_iters, gfs_step_stats *stats);
+// Accuracy of the last solve on this workspace: FP64 residual max|b - A p| of its
+// solution, and max|p - p_ref| / max|p_ref| against an FP64 PCG solve of the same
+// system to rel_tol (the workspace's pressure is left as it was).
+int pressure_check(Ctx *ctx, PressureWs &ws, const Grids &g, double density, double dt, double rel_tol,
+                   double *fp64_residual, double *rel_error, int *ref_iterations);
 // The system's flags, b and neighbour bits only (no solve).
 int pressure_setup(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat, float *const mac[3]);
 // Solve A x = rhs (padded cell layout, FP64) on the matrix of the last

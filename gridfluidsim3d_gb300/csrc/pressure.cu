@@ -1530,6 +1530,77 @@ int pressure_solve_rhs(Ctx *ctx, PressureWs &ws, const Grids &g, const double *r
     return GFS_OK;
 }
 
+// ------------------------------------------------- accuracy check
+
+__device__ __forceinline__ void atomic_max_nonneg(double *addr, double v) {
+    // non-negative doubles order like their bit patterns
+    atomicMax(reinterpret_cast<unsigned long long *>(addr), (unsigned long long)__double_as_longlong(v));
+}
+
+// out[0] = max |b - A p| (FP64, the matrix of the flags), out[1] = max |p - q|, out[2] = max |q|
+__global__ void __launch_bounds__(RED_THREADS) k_check(GridDim c, const uint8_t *__restrict__ flags,
+                                                       const double *__restrict__ b, const double *__restrict__ p,
+                                                       const double *__restrict__ q, double scale,
+                                                       double *__restrict__ out) {
+    double r = 0.0, e = 0.0, m = 0.0;
+    const long long sx = 1, sy = c.sx, sz = (long long)c.sx * c.sy;
+    for (long long at = blockIdx.x * (long long)blockDim.x + threadIdx.x; at < c.size;
+         at += (long long)gridDim.x * blockDim.x) {
+        uint8_t fl = flags[at];
+        if (!(fl & GFS_PF_FLUID)) continue;
+        // _applyMatrix (pressuresolver.cpp:388-426): diag*scale*x - scale * sum of fluid neighbours
+        double nb = 0.0;
+        const long long off[6] = {-sx, sx, -sy, sy, -sz, sz};
+        for (int k = 0; k < 6; k++)
+            if (flags[at + off[k]] & GFS_PF_FLUID) nb += p[at + off[k]];
+        double ap = (double)(fl >> 1) * scale * p[at] - scale * nb;
+        r = fmax(r, fabs(b[at] - ap));
+        e = fmax(e, fabs(p[at] - q[at]));
+        m = fmax(m, fabs(q[at]));
+    }
+    r = block_reduce<1>(r);
+    e = block_reduce<1>(e);
+    m = block_reduce<1>(m);
+    if (threadIdx.x == 0) {
+        atomic_max_nonneg(out, r);
+        atomic_max_nonneg(out + 1, e);
+        atomic_max_nonneg(out + 2, m);
+    }
+}
+
+int pressure_check(Ctx *ctx, PressureWs &ws, const Grids &g, double density, double dt, double rel_tol,
+                   double *fp64_residual, double *rel_error, int *ref_iterations) {
+    if (ws.allocated_for != g.c.size) {
+        set_error(GFS_ERR_STATE, "no pressure solve to check on this grid");
+        return GFS_ERR_STATE;
+    }
+    cudaStream_t st = ctx->stream;
+    const size_t bytes = (size_t)g.c.size * sizeof(double);
+    DevMem pm, bc, out;
+    if (pm.alloc(bytes) || bc.alloc(bytes) || out.alloc(3 * sizeof(double))) return GFS_ERR_NOMEM;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(pm.p, ws.p.p, bytes, cudaMemcpyDeviceToDevice, st));
+    GFS_CUDA_CHECK(cudaMemcpyAsync(bc.p, ws.b.p, bytes, cudaMemcpyDeviceToDevice, st));
+    gfs_step_stats stats{};
+    int rc = pressure_solve_rhs(ctx, ws, g, bc.as<double>(), density, dt, rel_tol, 20000, &stats);
+    if (rc) return rc;
+    GFS_CUDA_CHECK(cudaMemsetAsync(out.p, 0, out.bytes, st));
+    const double scale = dt / (density * g.dx * g.dx);
+    k_check<<<(unsigned)ws.nblocks_red, RED_THREADS, 0, st>>>(g.c, ws.flags.as<uint8_t>(), bc.as<double>(),
+                                                              pm.as<double>(), ws.p.as<double>(), scale,
+                                                              out.as<double>());
+    ctx->launches++;
+    GFS_LAUNCH_CHECK();
+    double h[3];
+    GFS_CUDA_CHECK(cudaMemcpyAsync(h, out.p, sizeof(h), cudaMemcpyDeviceToHost, st));
+    // the checked solution back in place (the workspace's pressure is the substep's)
+    GFS_CUDA_CHECK(cudaMemcpyAsync(ws.p.p, pm.p, bytes, cudaMemcpyDeviceToDevice, st));
+    GFS_CUDA_CHECK(cudaStreamSynchronize(st));
+    if (fp64_residual) *fp64_residual = h[0];
+    if (rel_error) *rel_error = h[2] > 0.0 ? h[1] / h[2] : 0.0;
+    if (ref_iterations) *ref_iterations = stats.cg_iterations;
+    return GFS_OK;
+}
+
 // ------------------------------------------------------ apply pressure
 
 struct ApplyArgs {

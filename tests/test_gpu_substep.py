@@ -104,3 +104,21 @@ def test_invalid_dt_raises(gpu_ctx):
     sim = FluidSimulation(*sc.dims, sc.dx, max_particles=sc.num_particles, ctx=gpu_ctx)
     with pytest.raises(GFSError):
         sim.update(-1.0)
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_pressure_check_against_fp64(gpu_ctx, precision):
+    """gfs_sim_pressure_check: the step's pressure against an FP64 solve of the same
+    system to 1e-12 -- the per-step error of the mixed form against the FP64 oracle."""
+    from gridfluidsim3d_gb300 import PRECISION_MIXED, PRECISION_PLAIN
+    sc = scenes.random_box(dims=(30, 22, 26), seed=3)
+    sim = FluidSimulation(*sc.dims, sc.dx, max_particles=sc.num_particles, ctx=gpu_ctx)
+    sim.precision = PRECISION_PLAIN if precision == "plain" else PRECISION_MIXED
+    sim.set_material_grid(sc.mat)
+    sim.set_marker_particles(sc.pos, sc.vel, sc.ids)
+    for _ in range(2):
+        sim.update(sc.dt)
+        chk = sim.pressure_check(sc.dt)
+        assert chk["fp64_residual"] < 1e-6
+        assert chk["rel_error"] < (1e-6 if precision == "plain" else 1e-5), chk
+    sim.close()
