@@ -231,6 +231,14 @@ int gfs_sim_step(gfs_sim *sim, double dt, gfs_step_stats *stats);
 int gfs_sim_step_host(gfs_sim *sim, double dt, float *h_positions, float *h_velocities,
                       uint32_t *h_ids, int64_t *n, gfs_step_stats *stats);
 
+/* Accuracy of the last step's pressure solve against FP64: the same system
+   (matrix and right-hand side of that step, dt its step length) is solved again
+   by FP64 MIC(0)-PCG to max|r| < rel_tol * max|b|; reports the FP64 residual
+   max|b - A p| of the step's solution p and max|p - p_ref| / max|p_ref|.  The
+   simulation's state is unchanged. */
+int gfs_sim_pressure_check(gfs_sim *sim, double dt, double rel_tol, double *fp64_residual,
+                           double *rel_error, int *ref_iterations);
+
 /* ------------------------------------------------ differentiable rollout */
 
 /* A differentiable rollout of `nsteps` substeps of length dt over n particles
