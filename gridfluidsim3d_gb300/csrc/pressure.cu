@@ -10,7 +10,9 @@
 // handles plane t forwards, plane S-1-t backwards).  The j / k neighbours were
 // produced by the adjacent threads one step earlier (shared-memory exchange,
 // one barrier per step), the i neighbour by the thread itself.  Per-cell
-// inputs are prefetched P steps ahead into registers.  Blocks hand their edge
+// inputs are prefetched P steps ahead (cp.async into shared memory for the
+// triangular solves, k_tri; registers for the build, k_sweep).  Blocks without
+// fluid are skipped: they hand over zeros only.  Blocks hand their edge
 // values to the downstream blocks through tagged 64-bit exchange words (value
 // bits | sweep epoch): a consumer prefetches the word it will need P steps
 // later and only re-reads it (bounded) if the tag is not yet this sweep's, so
@@ -439,40 +441,8 @@ struct Acc2f {
     __device__ __forceinline__ double value() const { return (double)s + (double)c; }
 };
 
-// ---- TMA bulk copies into a shared-memory ring, completion tracked by mbarriers
-
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// 1-D bulk copy global -> shared (16-byte aligned, size a multiple of 16)
-__device__ __forceinline__ void tma_load_1d(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_addr(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
-                 : "memory");
-}
-
-// Exchange words are read with an in-place L2 load (asm volatile keeps it where it is written).
 
 // In-place loads for the wavefront's prefetch ring: asm volatile keeps each load
 // where it is written (P steps before its use), so its latency overlaps the
@@ -1153,10 +1123,11 @@ static int launch_sweep(Ctx *ctx, PressureWs &ws, const T *in, T *out, const T *
     A.ctrl = C;
     A.init = init;
     ProfScope prof(ctx, MODE == SW_FWD ? KC_SWEEP_FWD : (MODE == SW_BWD ? KC_SWEEP_BWD : KC_PRECON));
-    if (MODE == SW_PRECON)
+    // the build runs k_sweep, the triangular solves k_tri (only the launched kernel is instantiated)
+    if constexpr (MODE == SW_PRECON)
         k_sweep<T, MODE, P, PE><<<A.K.nbj * A.K.nbk, SWEEP_THREADS, 0, ctx->stream>>>(A);
     else
-        k_tri<T, (MODE == SW_PRECON ? SW_FWD : MODE), P, PE><<<A.K.nbj * A.K.nbk, SPLANE, 0, ctx->stream>>>(A);
+        k_tri<T, MODE, P, PE><<<A.K.nbj * A.K.nbk, SPLANE, 0, ctx->stream>>>(A);
     ctx->launches++;
     GFS_LAUNCH_CHECK();
     return GFS_OK;
