@@ -914,25 +914,191 @@ __device__ __forceinline__ T neighbour_sum(const Skew &K, const T *__restrict__ 
     return Op::add(Op::add(Op::add(Op::add(Op::add(xim, xip), xjm), xjp), xkm), xkp);
 }
 
+// ------------------------------------------------- strip-wise vector kernels
+//
+// The per-iteration vector kernels take one strip per thread: 32 bytes of
+// consecutive slots of one row (fixed plane s and kl) of a pencil block -- 8
+// FP32 or 4 FP64 slots.  A strip costs one flag load and two 16-byte loads per
+// operand, all issued together, so the kernels stream at HBM rate instead of
+// waiting on a byte load before each slot's operands.  Strips without fluid are
+// skipped; stores stay per slot and on fluid slots only, so the results are those
+// of the slot-wise loops in the reference (pressuresolver.cpp:388-486) bit for bit.
+
+template <class T>
+struct Strip {
+    static constexpr int W = 32 / (int)sizeof(T);   // slots per strip
+    static constexpr int PER_ROW = SBJ / W, PER_PLANE = SPLANE / W;
+    static constexpr int NF = W / 4;                 // 32-bit flag words
+};
+
+struct StripPos {
+    int bj, bk, s, kl, jl0;
+    long long q0;   // first slot
+};
+
+template <class T>
+__device__ __forceinline__ StripPos strip_pos(const Skew &K, unsigned u) {
+    using St = Strip<T>;
+    const unsigned per = (unsigned)K.S * St::PER_PLANE;   // strips per pencil block
+    StripPos P;
+    const unsigned pb = u / per, rem = u - pb * per;
+    P.s = (int)(rem / St::PER_PLANE);
+    const unsigned w = rem - (unsigned)P.s * St::PER_PLANE;
+    P.kl = (int)(w / St::PER_ROW);
+    P.jl0 = (int)(w - (unsigned)P.kl * St::PER_ROW) * St::W;
+    P.bk = (int)(pb / (unsigned)K.nbj);
+    P.bj = (int)(pb - (unsigned)P.bk * K.nbj);
+    P.q0 = (long long)u * St::W;
+    return P;
+}
+
+template <class T>
+struct StripFlags {
+    unsigned w[Strip<T>::NF];
+    __device__ __forceinline__ void load(const uint8_t *fsk, long long q0) {
+        if constexpr (Strip<T>::NF == 2) {
+            const uint2 v = *reinterpret_cast<const uint2 *>(fsk + q0);
+            w[0] = v.x;
+            w[1] = v.y;
+        } else {
+            w[0] = *reinterpret_cast<const unsigned *>(fsk + q0);
+        }
+    }
+    __device__ __forceinline__ unsigned at(int e) const { return (w[e >> 2] >> (8 * (e & 3))) & 0xffu; }
+    __device__ __forceinline__ bool fluid(int e) const { return (at(e) & GFS_PF_FLUID) != 0u; }
+    __device__ __forceinline__ bool any() const {
+        unsigned o = 0u;
+#pragma unroll
+        for (int h = 0; h < Strip<T>::NF; h++) o |= w[h];
+        return (o & 0x01010101u) != 0u;
+    }
+    __device__ __forceinline__ bool all() const {
+        unsigned a = 0x01010101u;
+#pragma unroll
+        for (int h = 0; h < Strip<T>::NF; h++) a &= w[h];
+        return a == 0x01010101u;
+    }
+};
+
+// d[0..W-1] = p[0..W-1] (two 16-byte loads; p is 32-byte aligned), or 0 when !ok
+template <class T>
+__device__ __forceinline__ void load_strip(T (&d)[Strip<T>::W], const T *p, bool ok = true) {
+    if constexpr (sizeof(T) == 4) {
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+        if (ok) {
+            a = *reinterpret_cast<const float4 *>(p);
+            b = *reinterpret_cast<const float4 *>(p + 4);
+        }
+        d[0] = a.x; d[1] = a.y; d[2] = a.z; d[3] = a.w;
+        d[4] = b.x; d[5] = b.y; d[6] = b.z; d[7] = b.w;
+    } else {
+        double2 a = make_double2(0.0, 0.0), b = a;
+        if (ok) {
+            a = *reinterpret_cast<const double2 *>(p);
+            b = *reinterpret_cast<const double2 *>(p + 2);
+        }
+        d[0] = a.x; d[1] = a.y; d[2] = b.x; d[3] = b.y;
+    }
+}
+
+// p = d on the fluid slots of the strip (two 16-byte stores when all are fluid)
+template <class T>
+__device__ __forceinline__ void store_strip_fluid(T *p, const T (&d)[Strip<T>::W], const StripFlags<T> &f) {
+    if (f.all()) {
+        if constexpr (sizeof(T) == 4) {
+            *reinterpret_cast<float4 *>(p) = make_float4(d[0], d[1], d[2], d[3]);
+            *reinterpret_cast<float4 *>(p + 4) = make_float4(d[4], d[5], d[6], d[7]);
+        } else {
+            *reinterpret_cast<double2 *>(p) = make_double2(d[0], d[1]);
+            *reinterpret_cast<double2 *>(p + 2) = make_double2(d[2], d[3]);
+        }
+        return;
+    }
+#pragma unroll
+    for (int e = 0; e < Strip<T>::W; e++)
+        if (f.fluid(e)) p[e] = d[e];
+}
+
+// x at the six neighbours of each slot of a strip, summed in the reference's
+// order i-1, i+1, j-1, j+1, k-1, k+1 (0 outside the grid).  Neighbours in
+// plane s-1 / s+1 of the same pencil block are strip loads of the rows
+// (s-1, kl), (s+1, kl), (s-1, kl-1), (s+1, kl+1); j-1 / j+1 of slot jl are
+// rows (s-1, kl) / (s+1, kl) shifted by one, whose two outermost values are
+// scalar loads (from the adjacent pencil block at jl = 0 / 15).  Slots outside
+// the grid hold 0 in x, so a neighbour slot outside the grid reads 0; the
+// guards only keep the addresses inside the array.
+template <class T>
+__device__ __forceinline__ void neighbour_sum_strip(const Skew &K, const T *__restrict__ x, const StripPos &P,
+                                                    T (&sum)[Strip<T>::W]) {
+    using Op = Ar<T>;
+    constexpr int W = Strip<T>::W;
+    const long long q0 = P.q0;
+    const bool has_m = P.s > 0, has_p = P.s + 1 < K.S;
+    T im[W], ip[W], km[W], kp[W];
+    load_strip<T>(im, x + (has_m ? q0 - SPLANE : q0), has_m);
+    load_strip<T>(ip, x + (has_p ? q0 + SPLANE : q0), has_p);
+    T jm0 = T(0), jpl = T(0);
+    if (P.jl0 > 0) {
+        if (has_m) jm0 = x[q0 - SPLANE - 1];
+    } else if (P.bj > 0 && P.s + SBJ - 1 < K.S) {
+        jm0 = x[K.slot(P.bj - 1, P.bk, P.s + SBJ - 1, SBJ - 1, P.kl)];
+    }
+    if (P.jl0 + W < SBJ) {
+        if (has_p) jpl = x[q0 + SPLANE + W];
+    } else if (P.bj + 1 < K.nbj && P.s >= SBJ - 1) {
+        jpl = x[K.slot(P.bj + 1, P.bk, P.s - SBJ + 1, 0, P.kl)];
+    }
+    if (P.kl > 0) {
+        load_strip<T>(km, x + (has_m ? q0 - SPLANE - SBJ : q0), has_m);
+    } else {
+        const bool ok = P.bk > 0 && P.s + SBK - 1 < K.S;
+        load_strip<T>(km, x + (ok ? K.slot(P.bj, P.bk - 1, P.s + SBK - 1, P.jl0, SBK - 1) : 0), ok);
+    }
+    if (P.kl < SBK - 1) {
+        load_strip<T>(kp, x + (has_p ? q0 + SPLANE + SBJ : q0), has_p);
+    } else {
+        const bool ok = P.bk + 1 < K.nbk && P.s >= SBK - 1;
+        load_strip<T>(kp, x + (ok ? K.slot(P.bj, P.bk + 1, P.s - SBK + 1, P.jl0, 0) : 0), ok);
+    }
+#pragma unroll
+    for (int e = 0; e < W; e++) {
+        const T jm = e == 0 ? jm0 : im[e - 1];
+        const T jp = e == W - 1 ? jpl : ip[e + 1];
+        sum[e] = Op::add(Op::add(Op::add(Op::add(Op::add(im[e], ip[e]), jm), jp), km[e]), kp[e]);
+    }
+}
+
 // As = A s and dot(As, s) -> alpha (pressuresolver.cpp:388-426, :472-473)
 template <class T>
 __global__ void __launch_bounds__(RED_THREADS) k_matvec(VecArgs<T> A, const T *__restrict__ s,
                                                         T *__restrict__ As) {
     using Op = Ar<T>;
+    constexpr int W = Strip<T>::W;
     if (A.ctrl->done) return;
     const Skew &K = A.K;
     double dot = 0.0;   // FP64 operands
     Acc2f dot32;        // FP32 operands: compensated
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < K.size;
-         q += (long long)gridDim.x * blockDim.x) {
-        uint8_t fl = A.fsk[q];
-        if (!(fl & GFS_PF_FLUID)) continue;
-        T x = s[q];
-        T val = Op::mul(neighbour_sum<T>(K, s, q), A.negscale);
-        val = Op::add(val, Op::mul(Op::mul((T)(fl >> 1), A.scale), x));
-        As[q] = val;
-        if (sizeof(T) == 4) dot32.add((float)val * (float)x);
-        else dot += (double)val * (double)x;
+    const unsigned nstrip = (unsigned)(K.size / W);
+    for (unsigned u = blockIdx.x * blockDim.x + threadIdx.x; u < nstrip; u += gridDim.x * blockDim.x) {
+        const StripPos P = strip_pos<T>(K, u);
+        StripFlags<T> f;
+        f.load(A.fsk, P.q0);
+        if (!f.any()) continue;
+        T xc[W], val[W];
+        load_strip<T>(xc, s + P.q0);
+        neighbour_sum_strip<T>(K, s, P, val);
+#pragma unroll
+        for (int e = 0; e < W; e++) {
+            const unsigned fl = f.at(e);
+            T v = Op::mul(val[e], A.negscale);
+            v = Op::add(v, Op::mul(Op::mul((T)(fl >> 1), A.scale), xc[e]));
+            val[e] = v;
+            if (fl & GFS_PF_FLUID) {
+                if (sizeof(T) == 4) dot32.add((float)v * (float)xc[e]);
+                else dot += (double)v * (double)xc[e];
+            }
+        }
+        store_strip_fluid<T>(As + P.q0, val, f);
     }
     double part = block_reduce<0>(sizeof(T) == 4 ? dot32.value() : dot);
     double res;
@@ -945,17 +1111,30 @@ template <class T>
 __global__ void __launch_bounds__(RED_THREADS) k_axpy(VecArgs<T> A, T *__restrict__ p, T *__restrict__ r,
                                                       const T *__restrict__ s, const T *__restrict__ As) {
     using Op = Ar<T>;
+    constexpr int W = Strip<T>::W;
     PsCtrl *C = A.ctrl;
     if (C->done) return;
     const T alpha = (T)C->alpha, nalpha = (T)(-C->alpha);
     T mx = T(0);
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < A.K.size;
-         q += (long long)gridDim.x * blockDim.x) {
-        if (!(A.fsk[q] & GFS_PF_FLUID)) continue;
-        p[q] = Op::add(p[q], Op::mul(s[q], alpha));
-        T rv = Op::add(r[q], Op::mul(As[q], nalpha));
-        r[q] = rv;
-        mx = fmax(mx, fabs(rv));
+    const unsigned nstrip = (unsigned)(A.K.size / W);
+    for (unsigned u = blockIdx.x * blockDim.x + threadIdx.x; u < nstrip; u += gridDim.x * blockDim.x) {
+        const long long q0 = (long long)u * W;
+        StripFlags<T> f;
+        f.load(A.fsk, q0);
+        if (!f.any()) continue;
+        T pv[W], sv[W], rv[W], av[W];
+        load_strip<T>(pv, p + q0);
+        load_strip<T>(sv, s + q0);
+        load_strip<T>(rv, r + q0);
+        load_strip<T>(av, As + q0);
+#pragma unroll
+        for (int e = 0; e < W; e++) {
+            pv[e] = Op::add(pv[e], Op::mul(sv[e], alpha));
+            rv[e] = Op::add(rv[e], Op::mul(av[e], nalpha));
+            if (f.fluid(e)) mx = fmax(mx, fabs(rv[e]));
+        }
+        store_strip_fluid<T>(p + q0, pv, f);
+        store_strip_fluid<T>(r + q0, rv, f);
     }
     double part = block_reduce<1>((double)mx);
     double res;
@@ -974,12 +1153,21 @@ template <class T>
 __global__ void __launch_bounds__(RED_THREADS) k_update_s(VecArgs<T> A, const T *__restrict__ z,
                                                           T *__restrict__ s) {
     using Op = Ar<T>;
+    constexpr int W = Strip<T>::W;
     if (A.ctrl->done) return;
     const T beta = (T)A.ctrl->beta;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < A.K.size;
-         q += (long long)gridDim.x * blockDim.x) {
-        if (!(A.fsk[q] & GFS_PF_FLUID)) continue;
-        s[q] = Op::add(Op::mul(z[q], (T)1.0), Op::mul(s[q], beta));
+    const unsigned nstrip = (unsigned)(A.K.size / W);
+    for (unsigned u = blockIdx.x * blockDim.x + threadIdx.x; u < nstrip; u += gridDim.x * blockDim.x) {
+        const long long q0 = (long long)u * W;
+        StripFlags<T> f;
+        f.load(A.fsk, q0);
+        if (!f.any()) continue;
+        T zv[W], sv[W];
+        load_strip<T>(zv, z + q0);
+        load_strip<T>(sv, s + q0);
+#pragma unroll
+        for (int e = 0; e < W; e++) sv[e] = Op::add(Op::mul(zv[e], (T)1.0), Op::mul(sv[e], beta));
+        store_strip_fluid<T>(s + q0, sv, f);
     }
 }
 
