@@ -1194,6 +1194,31 @@ __global__ void __launch_bounds__(RED_THREADS) k_mixed_prepare(Skew K, const uin
     }
 }
 
+// MIXED, reliable update: the inner FP32 CG goes on with the true residual.
+// r32 = r64 (the FP64 residual of the corrected p64), e32 = 0, and the search
+// direction s32 and sigma are kept, so the Krylov information of the earlier
+// inner iterations is not thrown away.  The pending preconditioner apply of the
+// iteration that met the inner threshold completes that iteration, so the
+// iteration counter restarts at -1 (that apply brings it to 0).
+__global__ void __launch_bounds__(RED_THREADS) k_mixed_reliable(Skew K, const uint8_t *__restrict__ fsk,
+                                                                const double *__restrict__ r64,
+                                                                float *__restrict__ r32, float *__restrict__ e32,
+                                                                PsCtrl *ctrl, double eta) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < K.size;
+         q += (long long)gridDim.x * blockDim.x) {
+        bool f = fsk[q] & GFS_PF_FLUID;
+        r32[q] = f ? (float)r64[q] : 0.0f;
+        e32[q] = 0.0f;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        double m = ctrl->maxr64;
+        ctrl->inner_tol = fmax(eta * m, 0.25 * ctrl->tol);
+        ctrl->done = 0;
+        ctrl->converged = 0;
+        ctrl->iter = -1;
+    }
+}
+
 // MIXED: p64 += e32 (outer refinement)
 __global__ void __launch_bounds__(RED_THREADS) k_mixed_correct(Skew K, const uint8_t *__restrict__ fsk,
                                                                double *__restrict__ p64,
@@ -1371,6 +1396,9 @@ static int read_ctrl(Ctx *ctx, PressureWs &ws, PsCtrl *h) {
 }
 
 #define CG_CHUNK 8
+#ifndef GFS_MIXED_ETA
+#define GFS_MIXED_ETA 1e-2
+#endif
 
 int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat, float *const mac[3],
                    double density, double dt, int precision, double tol, int max_iters,
@@ -1458,7 +1486,8 @@ int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
             final_res = h.maxr;
             sweeps = 1 + h.iter;
         } else {
-            const double eta = 1e-3;
+            // inner FP32 rounds end when max|r32| has dropped below eta * max|r64| of the last update
+            const double eta = GFS_MIXED_ETA;
             float *r32 = ws.r32.as<float>(), *z32 = ws.z32.as<float>(), *s32 = ws.s32.as<float>(),
                   *As32 = ws.As32.as<float>(), *q32 = ws.q32.as<float>(), *e32 = ws.e32.as<float>(),
                   *pc32 = ws.precon32.as<float>();
@@ -1467,11 +1496,16 @@ int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
             double res64 = h.maxb;
             VecArgs<double> V64 = vec_args<double>(ws, scale, 1);
             VecArgs<float> V32 = vec_args<float>(ws, scale, 1);
+            bool first = true;
             while (total < max_iters) {
                 {
                     ProfScope prof(ctx, KC_MIXED_AUX);
-                    k_mixed_prepare<<<nb, RED_THREADS, 0, st>>>(K, ws.fsk.as<uint8_t>(), ws.r.as<double>(), r32,
-                                                               e32, s32, C, eta);
+                    if (first)
+                        k_mixed_prepare<<<nb, RED_THREADS, 0, st>>>(K, ws.fsk.as<uint8_t>(), ws.r.as<double>(), r32,
+                                                                   e32, s32, C, eta);
+                    else
+                        k_mixed_reliable<<<nb, RED_THREADS, 0, st>>>(K, ws.fsk.as<uint8_t>(), ws.r.as<double>(), r32,
+                                                                    e32, C, eta);
                 }
                 ctx->launches++;
                 // the inner cap is what is left of the total budget
@@ -1481,8 +1515,11 @@ int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
                 }
                 rc = launch_sweep<float, SW_FWD>(ctx, ws, r32, q32, pc32, nullptr, nullptr, scale, 0);
                 if (rc) return rc;
-                rc = launch_sweep<float, SW_BWD>(ctx, ws, q32, z32, pc32, r32, nullptr, scale, 1);
+                // first round: s = z = M^-1 r (init); later rounds: the pending half of the
+                // iteration that met the inner threshold, beta = sigma_new / sigma, s = z + beta s
+                rc = launch_sweep<float, SW_BWD>(ctx, ws, q32, z32, pc32, r32, nullptr, scale, first ? 1 : 0);
                 if (rc) return rc;
+                first = false;
                 {
                     ProfScope prof(ctx, KC_UPDATE_S);
                     k_update_s<float><<<nb, RED_THREADS, 0, st>>>(V32, z32, s32);
