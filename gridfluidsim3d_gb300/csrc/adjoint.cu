@@ -928,7 +928,10 @@ int diff_backward(DiffRun *d, const float *d_rho_bar, const float *d_grad_centro
         ctx->launches++;
         GFS_LAUNCH_CHECK();
         gfs_step_stats ps{};
-        if ((rc = pressure_solve_rhs(ctx, s->ps, g, d->pbar.as<double>(), s->params.density, d->dt, 1e-7, 2000, &ps)))
+        // the adjoint system has the forward's matrix; it is solved in the forward's precision form
+        // (MIXED: FP32 inner PCG with FP64 residual updates) to the same FP64 residual rule
+        if ((rc = pressure_solve_rhs(ctx, s->ps, g, d->pbar.as<double>(), s->params.density, d->dt, 1e-7, 2000, &ps,
+                                     s->params.precision == GFS_PRECISION_MIXED)))
             return rc;
         k_adj_div<<<face_grid(g.c), face_block(), 0, st>>>(P, s->mat.as<uint8_t>(), s->ps.p.as<double>(),
                                                           d->g0[0].as<float>(), d->g0[1].as<float>(),

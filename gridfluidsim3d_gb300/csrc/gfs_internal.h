@@ -182,7 +182,7 @@ int pressure_setup(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
 // pressure_solve on this workspace, to max|r| < rel_tol * max|rhs|; the
 // solution is left in ws.p.
 int pressure_solve_rhs(Ctx *ctx, PressureWs &ws, const Grids &g, const double *rhs, double density, double dt,
-                       double rel_tol, int max_iters, gfs_step_stats *stats);
+                       double rel_tol, int max_iters, gfs_step_stats *stats, bool mixed = false);
 int pressure_apply(Sim *s, double dt);
 int pressure_to_grid(Ctx *ctx, PressureWs &ws, const Grids &g, float *pgrid_unpadded);
 int pressure_gather_compact(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,

@@ -1400,6 +1400,131 @@ static int read_ctrl(Ctx *ctx, PressureWs &ws, PsCtrl *h) {
 #define GFS_MIXED_ETA 1e-2
 #endif
 
+// MICCG(0) on the system set up in ws (b, r = b, p = s = 0 in the skewed layout,
+// control block reset by the set-up kernel), to max|r| < tol or max_iters:
+// PLAIN is the reference's FP64 PCG (pressuresolver.cpp:448-498); MIXED runs the
+// inner PCG in FP32 with FP64 reliable updates of the residual.  Fills the
+// reference-numbered iteration count, the final max-norm residual, the number
+// of FP64 updates and of forward (= backward) MIC(0) solves.
+static int run_cg(Ctx *ctx, PressureWs &ws, const Skew &K, double scale, bool mixed, double tol, int max_iters,
+                  PsCtrl &h, int &iterations, double &final_res, int &refinements, int &sweeps) {
+    cudaStream_t st = ctx->stream;
+    PsCtrl *C = ws.ctrl.as<PsCtrl>();
+    unsigned nb = (unsigned)ws.nblocks_red;
+    int rc = GFS_OK;
+    // MIC(0) preconditioner (pressuresolver.cpp:246-302): FP64 for PLAIN, FP32 for the MIXED inner solve
+    if (mixed) rc = launch_sweep<float, SW_PRECON>(ctx, ws, nullptr, ws.precon32.as<float>(), nullptr, nullptr,
+                                                   nullptr, scale, 0);
+    else rc = launch_sweep<double, SW_PRECON>(ctx, ws, nullptr, ws.precon.as<double>(), nullptr, nullptr, nullptr,
+                                              scale, 0);
+    if (rc) return rc;
+    if (!mixed) {
+        double *p = ws.psk.as<double>(), *r = ws.r.as<double>(), *z = ws.z.as<double>(),
+               *s = ws.s.as<double>(), *As = ws.As.as<double>(), *q = ws.q.as<double>(),
+               *pc = ws.precon.as<double>();
+        rc = launch_sweep<double, SW_FWD>(ctx, ws, r, q, pc, nullptr, nullptr, scale, 0);
+        if (rc) return rc;
+        rc = launch_sweep<double, SW_BWD>(ctx, ws, q, z, pc, r, nullptr, scale, 1);
+        if (rc) return rc;
+        VecArgs<double> V = vec_args<double>(ws, scale, 0);
+        {
+            ProfScope prof(ctx, KC_UPDATE_S);
+            k_update_s<double><<<nb, RED_THREADS, 0, st>>>(V, z, s);
+        }
+        ctx->launches++;
+        for (;;) {
+            for (int it = 0; it < CG_CHUNK; it++) {
+                rc = cg_iteration<double>(ctx, ws, scale, 0, p, r, z, s, As, q, pc);
+                if (rc) return rc;
+            }
+            rc = read_ctrl(ctx, ws, &h);
+            if (rc) return rc;
+            if (h.done) break;
+        }
+        iterations = h.iter;
+        final_res = h.maxr;
+        sweeps = 1 + h.iter;
+    } else {
+        // inner FP32 rounds end when max|r32| has dropped below eta * max|r64| of the last update
+        const double eta = GFS_MIXED_ETA;
+        float *r32 = ws.r32.as<float>(), *z32 = ws.z32.as<float>(), *s32 = ws.s32.as<float>(),
+              *As32 = ws.As32.as<float>(), *q32 = ws.q32.as<float>(), *e32 = ws.e32.as<float>(),
+              *pc32 = ws.precon32.as<float>();
+        int total = 0;
+        bool converged = false;
+        double res64 = h.maxb;
+        VecArgs<double> V64 = vec_args<double>(ws, scale, 1);
+        VecArgs<float> V32 = vec_args<float>(ws, scale, 1);
+        bool first = true;
+        while (total < max_iters) {
+            {
+                ProfScope prof(ctx, KC_MIXED_AUX);
+                if (first)
+                    k_mixed_prepare<<<nb, RED_THREADS, 0, st>>>(K, ws.fsk.as<uint8_t>(), ws.r.as<double>(), r32,
+                                                               e32, s32, C, eta);
+                else
+                    k_mixed_reliable<<<nb, RED_THREADS, 0, st>>>(K, ws.fsk.as<uint8_t>(), ws.r.as<double>(), r32,
+                                                                e32, C, eta);
+            }
+            ctx->launches++;
+            // the inner cap is what is left of the total budget
+            {
+                int left = max_iters - total;
+                GFS_CUDA_CHECK(cudaMemcpyAsync(&C->max_iters, &left, sizeof(int), cudaMemcpyHostToDevice, st));
+            }
+            rc = launch_sweep<float, SW_FWD>(ctx, ws, r32, q32, pc32, nullptr, nullptr, scale, 0);
+            if (rc) return rc;
+            // first round: s = z = M^-1 r (init); later rounds: the pending half of the
+            // iteration that met the inner threshold, beta = sigma_new / sigma, s = z + beta s
+            rc = launch_sweep<float, SW_BWD>(ctx, ws, q32, z32, pc32, r32, nullptr, scale, first ? 1 : 0);
+            if (rc) return rc;
+            first = false;
+            {
+                ProfScope prof(ctx, KC_UPDATE_S);
+                k_update_s<float><<<nb, RED_THREADS, 0, st>>>(V32, z32, s32);
+            }
+            ctx->launches++;
+            for (;;) {
+                for (int it = 0; it < CG_CHUNK; it++) {
+                    rc = cg_iteration<float>(ctx, ws, scale, 1, e32, r32, z32, s32, As32, q32, pc32);
+                    if (rc) return rc;
+                }
+                rc = read_ctrl(ctx, ws, &h);
+                if (rc) return rc;
+                if (h.done) break;
+            }
+            // h.iter counts the inner iterations that completed without converging;
+            // the converging iteration is one more.
+            total += h.converged ? h.iter + 1 : h.iter;
+            sweeps += 1 + h.iter;
+            {
+                ProfScope prof(ctx, KC_MIXED_AUX);
+                k_mixed_correct<<<nb, RED_THREADS, 0, st>>>(K, ws.fsk.as<uint8_t>(), ws.psk.as<double>(), e32);
+                k_residual64<<<nb, RED_THREADS, 0, st>>>(V64, ws.bsk.as<double>(), ws.psk.as<double>(),
+                                                          ws.r.as<double>());
+            }
+            ctx->launches += 2;
+            rc = read_ctrl(ctx, ws, &h);
+            if (rc) return rc;
+            res64 = h.maxr64;
+            refinements = h.refinements;
+            if (res64 < tol) {
+                converged = true;
+                break;
+            }
+        }
+        // reference numbering: the converging iteration is not counted
+        iterations = converged ? total - 1 : total;
+        if (iterations < 0) iterations = 0;
+        final_res = res64;
+        // restore the cap for later solves
+        GFS_CUDA_CHECK(cudaMemcpyAsync(&C->max_iters, &max_iters, sizeof(int), cudaMemcpyHostToDevice, st));
+        int one = 1;
+        GFS_CUDA_CHECK(cudaMemcpyAsync(&C->done, &one, sizeof(int), cudaMemcpyHostToDevice, st));
+    }
+    return GFS_OK;
+}
+
 int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat, float *const mac[3],
                    double density, double dt, int precision, double tol, int max_iters,
                    gfs_step_stats *stats) {
@@ -1453,116 +1578,8 @@ int pressure_solve(Ctx *ctx, PressureWs &ws, const Grids &g, const uint8_t *mat,
     int refinements = 0;
     int sweeps = 0;   // forward (= backward) MIC(0) solves that did work
     if (!h.done) {
-        // MIC(0) preconditioner (pressuresolver.cpp:246-302), FP64 in both modes
-        if (mixed) rc = launch_sweep<float, SW_PRECON>(ctx, ws, nullptr, ws.precon32.as<float>(), nullptr, nullptr,
-                                                       nullptr, scale, 0);
-        else rc = launch_sweep<double, SW_PRECON>(ctx, ws, nullptr, ws.precon.as<double>(), nullptr, nullptr, nullptr,
-                                                  scale, 0);
+        rc = run_cg(ctx, ws, K, scale, mixed, tol, max_iters, h, iterations, final_res, refinements, sweeps);
         if (rc) return rc;
-        if (!mixed) {
-            double *p = ws.psk.as<double>(), *r = ws.r.as<double>(), *z = ws.z.as<double>(),
-                   *s = ws.s.as<double>(), *As = ws.As.as<double>(), *q = ws.q.as<double>(),
-                   *pc = ws.precon.as<double>();
-            rc = launch_sweep<double, SW_FWD>(ctx, ws, r, q, pc, nullptr, nullptr, scale, 0);
-            if (rc) return rc;
-            rc = launch_sweep<double, SW_BWD>(ctx, ws, q, z, pc, r, nullptr, scale, 1);
-            if (rc) return rc;
-            VecArgs<double> V = vec_args<double>(ws, scale, 0);
-            {
-                ProfScope prof(ctx, KC_UPDATE_S);
-                k_update_s<double><<<nb, RED_THREADS, 0, st>>>(V, z, s);
-            }
-            ctx->launches++;
-            for (;;) {
-                for (int it = 0; it < CG_CHUNK; it++) {
-                    rc = cg_iteration<double>(ctx, ws, scale, 0, p, r, z, s, As, q, pc);
-                    if (rc) return rc;
-                }
-                rc = read_ctrl(ctx, ws, &h);
-                if (rc) return rc;
-                if (h.done) break;
-            }
-            iterations = h.iter;
-            final_res = h.maxr;
-            sweeps = 1 + h.iter;
-        } else {
-            // inner FP32 rounds end when max|r32| has dropped below eta * max|r64| of the last update
-            const double eta = GFS_MIXED_ETA;
-            float *r32 = ws.r32.as<float>(), *z32 = ws.z32.as<float>(), *s32 = ws.s32.as<float>(),
-                  *As32 = ws.As32.as<float>(), *q32 = ws.q32.as<float>(), *e32 = ws.e32.as<float>(),
-                  *pc32 = ws.precon32.as<float>();
-            int total = 0;
-            bool converged = false;
-            double res64 = h.maxb;
-            VecArgs<double> V64 = vec_args<double>(ws, scale, 1);
-            VecArgs<float> V32 = vec_args<float>(ws, scale, 1);
-            bool first = true;
-            while (total < max_iters) {
-                {
-                    ProfScope prof(ctx, KC_MIXED_AUX);
-                    if (first)
-                        k_mixed_prepare<<<nb, RED_THREADS, 0, st>>>(K, ws.fsk.as<uint8_t>(), ws.r.as<double>(), r32,
-                                                                   e32, s32, C, eta);
-                    else
-                        k_mixed_reliable<<<nb, RED_THREADS, 0, st>>>(K, ws.fsk.as<uint8_t>(), ws.r.as<double>(), r32,
-                                                                    e32, C, eta);
-                }
-                ctx->launches++;
-                // the inner cap is what is left of the total budget
-                {
-                    int left = max_iters - total;
-                    GFS_CUDA_CHECK(cudaMemcpyAsync(&C->max_iters, &left, sizeof(int), cudaMemcpyHostToDevice, st));
-                }
-                rc = launch_sweep<float, SW_FWD>(ctx, ws, r32, q32, pc32, nullptr, nullptr, scale, 0);
-                if (rc) return rc;
-                // first round: s = z = M^-1 r (init); later rounds: the pending half of the
-                // iteration that met the inner threshold, beta = sigma_new / sigma, s = z + beta s
-                rc = launch_sweep<float, SW_BWD>(ctx, ws, q32, z32, pc32, r32, nullptr, scale, first ? 1 : 0);
-                if (rc) return rc;
-                first = false;
-                {
-                    ProfScope prof(ctx, KC_UPDATE_S);
-                    k_update_s<float><<<nb, RED_THREADS, 0, st>>>(V32, z32, s32);
-                }
-                ctx->launches++;
-                for (;;) {
-                    for (int it = 0; it < CG_CHUNK; it++) {
-                        rc = cg_iteration<float>(ctx, ws, scale, 1, e32, r32, z32, s32, As32, q32, pc32);
-                        if (rc) return rc;
-                    }
-                    rc = read_ctrl(ctx, ws, &h);
-                    if (rc) return rc;
-                    if (h.done) break;
-                }
-                // h.iter counts the inner iterations that completed without converging;
-                // the converging iteration is one more.
-                total += h.converged ? h.iter + 1 : h.iter;
-                sweeps += 1 + h.iter;
-                {
-                    ProfScope prof(ctx, KC_MIXED_AUX);
-                    k_mixed_correct<<<nb, RED_THREADS, 0, st>>>(K, ws.fsk.as<uint8_t>(), ws.psk.as<double>(), e32);
-                    k_residual64<<<nb, RED_THREADS, 0, st>>>(V64, ws.bsk.as<double>(), ws.psk.as<double>(),
-                                                              ws.r.as<double>());
-                }
-                ctx->launches += 2;
-                rc = read_ctrl(ctx, ws, &h);
-                if (rc) return rc;
-                res64 = h.maxr64;
-                refinements = h.refinements;
-                if (res64 < tol) {
-                    converged = true;
-                    break;
-                }
-            }
-            // reference numbering: the converging iteration is not counted
-            iterations = converged ? total - 1 : total;
-            if (iterations < 0) iterations = 0;
-            final_res = res64;
-            // restore the cap for later solves
-            GFS_CUDA_CHECK(cudaMemcpyAsync(&C->max_iters, &max_iters, sizeof(int), cudaMemcpyHostToDevice, st));
-            int one = 1;
-            GFS_CUDA_CHECK(cudaMemcpyAsync(&C->done, &one, sizeof(int), cudaMemcpyHostToDevice, st));
-        }
     }
     // solution back to the padded cell layout
     {
@@ -1644,10 +1661,14 @@ __global__ void __launch_bounds__(RED_THREADS) k_set_rhs(GridDim c, const uint8_
 }
 
 int pressure_solve_rhs(Ctx *ctx, PressureWs &ws, const Grids &g, const double *rhs, double density, double dt,
-                       double rel_tol, int max_iters, gfs_step_stats *stats) {
+                       double rel_tol, int max_iters, gfs_step_stats *stats, bool mixed) {
     if (ws.allocated_for != g.c.size) {
         set_error(GFS_ERR_STATE, "pressure_solve_rhs needs a pressure solve on this grid first");
         return GFS_ERR_STATE;
+    }
+    if (mixed) {
+        int rc0 = ensure_ws(ctx, ws, g, true);
+        if (rc0) return rc0;
     }
     cudaStream_t st = ctx->stream;
     const double dx = g.dx;
@@ -1680,32 +1701,11 @@ int pressure_solve_rhs(Ctx *ctx, PressureWs &ws, const Grids &g, const double *r
     PsCtrl h;
     int rc = read_ctrl(ctx, ws, &h);
     if (rc) return rc;
-    int sweeps = 0;
+    int sweeps = 0, iterations = h.iter, refinements = 0;
+    double final_res = h.maxb;
     if (!h.done) {
-        double *p = ws.psk.as<double>(), *r = ws.r.as<double>(), *z = ws.z.as<double>(), *s = ws.s.as<double>(),
-               *As = ws.As.as<double>(), *q = ws.q.as<double>(), *pc = ws.precon.as<double>();
-        rc = launch_sweep<double, SW_PRECON>(ctx, ws, nullptr, pc, nullptr, nullptr, nullptr, scale, 0);
+        rc = run_cg(ctx, ws, K, scale, mixed, h.tol, max_iters, h, iterations, final_res, refinements, sweeps);
         if (rc) return rc;
-        rc = launch_sweep<double, SW_FWD>(ctx, ws, r, q, pc, nullptr, nullptr, scale, 0);
-        if (rc) return rc;
-        rc = launch_sweep<double, SW_BWD>(ctx, ws, q, z, pc, r, nullptr, scale, 1);
-        if (rc) return rc;
-        VecArgs<double> V = vec_args<double>(ws, scale, 0);
-        {
-            ProfScope prof(ctx, KC_UPDATE_S);
-            k_update_s<double><<<nb, RED_THREADS, 0, st>>>(V, z, s);
-        }
-        ctx->launches++;
-        for (;;) {
-            for (int it = 0; it < CG_CHUNK; it++) {
-                rc = cg_iteration<double>(ctx, ws, scale, 0, p, r, z, s, As, q, pc);
-                if (rc) return rc;
-            }
-            rc = read_ctrl(ctx, ws, &h);
-            if (rc) return rc;
-            if (h.done) break;
-        }
-        sweeps = 1 + h.iter;
     }
     {
         dim3 grid(grid_blocks(g.c.nx, 128), g.c.ny, g.c.nz);
@@ -1718,9 +1718,9 @@ int pressure_solve_rhs(Ctx *ctx, PressureWs &ws, const Grids &g, const double *r
         return GFS_ERR_TIMEOUT;
     }
     if (stats) {
-        stats->cg_iterations = h.iter;
-        stats->cg_max_residual = h.maxr;
-        stats->refinements = 0;
+        stats->cg_iterations = iterations;
+        stats->cg_max_residual = final_res;
+        stats->refinements = refinements;
         stats->sweeps = sweeps;
     }
     return GFS_OK;
