@@ -24,6 +24,8 @@ cpu_baseline  the oracle (C restatement of the reference's CPU path, single
 accuracy_vs_fp64  per timed substep (re-run untimed): max|p - p_ref| / max|p_ref|
            against an FP64 PCG solve of the same system to 1e-12, and the FP64
            residual max|b - A p| of the step's pressure, for both forms.
+savestate  FluidSimulationSaveState write / read of the whole state (GB/s), with the
+           oracle's CPU writer beside it.
 adjoint    fwd+adjoint ms/substep and peak HBM of the two differentiable
            configurations (32^3 cube, 20 substeps, MAC-field parameters; 128^3
            dam break, 60 substeps, per-particle velocities, Adam steps).
@@ -303,6 +305,41 @@ def profile_read(ctx):
     return out
 
 
+def savestate_bench(sim):
+    """FluidSimulationSaveState write and read of the simulation's current state
+    (all particles and solid cells of the 256^3 scene) through gfs_sim_save_state /
+    gfs_sim_load_state, to a file in the box's temporary directory: GB/s of file
+    bytes, wall clock around each call.  cpu_write: the same file written from host
+    arrays by the oracle's restatement of the reference's writer (the CPU path,
+    which first needs the particles on the host)."""
+    import tempfile
+    import oracle.savestate as OS
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "bench.state")
+        try:
+            t0 = time.perf_counter()
+            sim.save_state(path, current_frame=0)
+            t_save = time.perf_counter() - t0
+            size = os.path.getsize(path)
+            t0 = time.perf_counter()
+            sim.load_state(path)
+            t_load = time.perf_counter() - t0
+            pos, vel, _ = sim.get_marker_particles()
+            mat = sim.get_material_grid()
+            t0 = time.perf_counter()
+            OS.write_state(os.path.join(d, "cpu.state"), (sim.isize, sim.jsize, sim.ksize), sim.dx, 0, pos, vel, mat)
+            t_cpu = time.perf_counter() - t0
+        except Exception as e:   # a full disk or similar: report, do not fail the bench
+            return {"error": str(e)[:200]}
+        out = {"file_bytes": size, "particles": int(len(pos)), "save_s": round(t_save, 3),
+               "save_gbs": round(size / t_save / 1e9, 3), "load_s": round(t_load, 3),
+               "load_gbs": round(size / t_load / 1e9, 3), "cpu_write_s": round(t_cpu, 3),
+               "cpu_write_gbs": round(size / t_cpu / 1e9, 3),
+               "note": "wall clock around each call; includes the file system of the box"}
+    return out
+
+
 def adjoint_bench(ctx, iters=2, warmup=1):
     """fwd+adjoint ms/step of the two differentiable configurations.
 
@@ -478,6 +515,9 @@ def main(args):
     ctx.synchronize()
     te = reduce_max(time.perf_counter() - t0, world)
 
+    savestate = None
+    if r == 0 and world == 1 and not args.no_savestate and set(forms) == {"plain", "mixed"}:
+        savestate = savestate_bench(sim)
     adjoint = None
     if r == 0 and world == 1 and not args.no_adjoint and set(forms) == {"plain", "mixed"}:
         sim.close()
@@ -559,6 +599,7 @@ def main(args):
             "cpu_baseline": cpu,
             "clocks": clocks,
             "adjoint": adjoint,
+            "savestate": savestate,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -578,6 +619,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-rollout leg")
     ap.add_argument("--no-check", action="store_true", help="skip the per-step FP64 pressure check")
+    ap.add_argument("--no-savestate", action="store_true", help="skip the savestate write/read leg")
     ap.add_argument("--ref-cg-iterations", type=int, default=200,
                     help="CG iterations the reference arm scales its per-iteration cost to")
     a = ap.parse_args()

@@ -8,8 +8,9 @@ does, and there is no CPU fallback.
 """
 from ._lib import GFSError, PRECISION_MIXED, PRECISION_PLAIN  # noqa: F401
 from .core import (AIR, FLUID, SOLID, CLScalarField, Context, FluidSimulation,  # noqa: F401
-                   MACVelocityField, ParticleAdvector, PressureSolver, PressureSolverParameters, face_shape)
+                   FluidSimulationSaveState, MACVelocityField, ParticleAdvector, PressureSolver,
+                   PressureSolverParameters, face_shape)
 
 __all__ = ["GFSError", "PRECISION_PLAIN", "PRECISION_MIXED", "AIR", "FLUID", "SOLID", "Context",
            "CLScalarField", "ParticleAdvector", "PressureSolver", "PressureSolverParameters",
-           "MACVelocityField", "FluidSimulation", "face_shape"]
+           "MACVelocityField", "FluidSimulation", "FluidSimulationSaveState", "face_shape"]

@@ -89,6 +89,11 @@ _SIGNATURES = {
     "gfs_sim_step": [_P, _D, ctypes.POINTER(StepStats)],
     "gfs_sim_step_host": [_P, _D, _P, _P, _P, ctypes.POINTER(_I64), ctypes.POINTER(StepStats)],
     "gfs_sim_pressure_check": [_P, _D, _D, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_I)],
+    "gfs_savestate_read_header": [ctypes.c_char_p, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
+                                  ctypes.POINTER(_D), ctypes.POINTER(_I), ctypes.POINTER(_I64),
+                                  ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I)],
+    "gfs_sim_save_state": [_P, ctypes.c_char_p, _I],
+    "gfs_sim_load_state": [_P, ctypes.c_char_p, ctypes.POINTER(_I)],
     "gfs_diff_create": [_P, _I, _I64, _D, ctypes.POINTER(_P)],
     "gfs_diff_destroy": [_P],
     "gfs_diff_forward": [_P, _P, _P, _P, _P, _P, _P, _P],

@@ -22,6 +22,7 @@ raises RuntimeError from its bindings.
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 
@@ -432,6 +433,35 @@ class FluidSimulation:
         _lib.lib().gfs_sim_get_pressure_grid(self._h, _p(out))
         return out
 
+    # -- savestates (FluidSimulationSaveState file format) --
+    def save_state(self, filename, current_frame=None):
+        """FluidSimulation.save_state (pyfluid/fluidsimulation.py:109-113): the
+        marker particles and solid cells in the reference's savestate format."""
+        frame = self.current_frame if current_frame is None else int(current_frame)
+        _lib.lib().gfs_sim_save_state(self._h, os.fsencode(filename), frame)
+
+    def load_state(self, filename) -> int:
+        """Replace the material grid and particles by a savestate's (grid must
+        match); returns and adopts the file's current frame."""
+        frame = ctypes.c_int(0)
+        _lib.lib().gfs_sim_load_state(self._h, os.fsencode(filename), ctypes.byref(frame))
+        self.current_frame = frame.value
+        return frame.value
+
+    @classmethod
+    def from_save_state(cls, savestate, max_particles=None, ctx: Context | None = None):
+        """FluidSimulation.from_save_state (pyfluid/fluidsimulation.py:67-75): a
+        simulation with the savestate's grid, solid cells, particles and frame.
+        `savestate` is a FluidSimulationSaveState or a file name."""
+        st = savestate if isinstance(savestate, FluidSimulationSaveState) else FluidSimulationSaveState()
+        if st is not savestate:
+            st.load_state(savestate)
+        i, j, k = st.get_grid_dimensions()
+        cap = max(int(max_particles or 0), st.get_num_marker_particles(), 1)
+        sim = cls(i, j, k, st.get_cell_size(), cap, ctx=ctx)
+        sim.load_state(st.filename)
+        return sim
+
     # -- stepping --
     def update(self, dt) -> dict:
         """One substep of length dt (FluidSimulation::update, fluidsimulation.cpp:3417-3455)."""
@@ -471,3 +501,57 @@ class FluidSimulation:
             self.close()
         except Exception:
             pass
+
+
+class FluidSimulationSaveState:
+    """The header of a savestate file, as pyfluid's FluidSimulationSaveState
+    (pyfluid/fluidsimulationsavestate.py:18-207) reports it after load_state."""
+
+    def __init__(self):
+        self.filename = None
+        self._h = None
+
+    def load_state(self, filename) -> bool:
+        i, j, k, fr, br = (ctypes.c_int() for _ in range(5))
+        dx = ctypes.c_double()
+        nm, nd, ns = (ctypes.c_int64() for _ in range(3))
+        _lib.lib().gfs_savestate_read_header(os.fsencode(filename), ctypes.byref(i), ctypes.byref(j), ctypes.byref(k),
+                                             ctypes.byref(dx), ctypes.byref(fr), ctypes.byref(nm), ctypes.byref(nd),
+                                             ctypes.byref(ns), ctypes.byref(br))
+        self.filename = filename
+        self._h = dict(dims=(i.value, j.value, k.value), dx=dx.value, frame=fr.value, marker=nm.value,
+                       diffuse=nd.value, solid=ns.value, brick=bool(br.value))
+        return True
+
+    def close_state(self):
+        self.filename = None
+        self._h = None
+
+    def is_load_state_initialized(self) -> bool:
+        return self._h is not None
+
+    def _hdr(self):
+        if self._h is None:
+            raise GFSError(_lib.GFS_ERR_STATE, "FluidSimulationSaveState", "no state is loaded")
+        return self._h
+
+    def get_grid_dimensions(self):
+        return self._hdr()["dims"]
+
+    def get_cell_size(self):
+        return self._hdr()["dx"]
+
+    def get_current_frame(self):
+        return self._hdr()["frame"]
+
+    def get_num_marker_particles(self):
+        return self._hdr()["marker"]
+
+    def get_num_diffuse_particles(self):
+        return self._hdr()["diffuse"]
+
+    def get_num_solid_cells(self):
+        return self._hdr()["solid"]
+
+    def is_fluid_brick_grid_enabled(self):
+        return self._hdr()["brick"]

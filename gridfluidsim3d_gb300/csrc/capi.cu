@@ -266,6 +266,49 @@ static int sim_set_particles(Sim *s, const float *hp, const float *hv, const uin
     return GFS_OK;
 }
 
+// Device-side staging of the particle set as xyz triples (positions in pos_alt,
+// velocities in vel_alt, ids in key), for readers and writers of host formats.
+// Unpack: the current particles into the staging buffers, *n_out their count.
+int sim_stage_xyz(Sim *s, int64_t *n_out) {
+    Ctx *ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    uint32_t hn = 0;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(&hn, s->num.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GFS_CUDA_CHECK(cudaStreamSynchronize(st));
+    *n_out = hn;
+    if (hn > 0) {
+        k_unpack_particles<<<grid_blocks(hn, 256), 256, 0, st>>>(s->pos.as<float4>(), s->vel.as<float4>(), hn,
+                                                                 s->pos_alt.as<float>(), s->vel_alt.as<float>(),
+                                                                 s->key.as<uint32_t>());
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+    }
+    return GFS_OK;
+}
+
+// Pack: n staged xyz triples (ids 0..n-1) become the particle set, sorted by
+// (cell, id) with the particles in solid cells removed, as set_particles does.
+int sim_unstage_xyz(Sim *s, int64_t n) {
+    Ctx *ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    if (n < 0 || n > s->capacity) {
+        set_error(GFS_ERR_INVALID, "particle count %lld outside [0, capacity %lld]", (long long)n,
+                  (long long)s->capacity);
+        return GFS_ERR_INVALID;
+    }
+    if (n > 0) {
+        k_pack_particles<<<grid_blocks(n, 256), 256, 0, st>>>(s->pos_alt.as<float>(), s->vel_alt.as<float>(),
+                                                              nullptr, n, s->pos.as<float4>(), s->vel.as<float4>());
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+    }
+    uint32_t hn = (uint32_t)n;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(s->num.p, &hn, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    s->n_bound = n;
+    s->need_sort = true;
+    return sort_particles(s, true);
+}
+
 static int sim_get_particles(Sim *s, float *hp, float *hv, uint32_t *hid, int64_t *n_out) {
     Ctx *ctx = s->ctx;
     cudaStream_t st = ctx->stream;

@@ -145,6 +145,8 @@ int face_fill(Sim *s, double dt);     // a3 + saved copy + body forces
 
 // ---- capi.cu
 int sim_step(Sim *s, double dt, gfs_step_stats *stats);   // one device-resident substep
+int sim_stage_xyz(Sim *s, int64_t *n_out);   // particles -> xyz triples in pos_alt / vel_alt (ids in key)
+int sim_unstage_xyz(Sim *s, int64_t n);      // n staged triples (ids 0..n-1) -> particles, sorted
 
 // ---- adjoint.cu: the differentiable rollout
 struct DiffRun;

@@ -239,6 +239,37 @@ int gfs_sim_step_host(gfs_sim *sim, double dt, float *h_positions, float *h_velo
 int gfs_sim_pressure_check(gfs_sim *sim, double dt, double rel_tol, double *fp64_residual,
                            double *rel_error, int *ref_iterations);
 
+/* ------------------------------------------------------------- savestates */
+
+/* The header of a FluidSimulationSaveState file
+   (FluidSimulationSaveState::loadState, fluidsimulationsavestate.cpp:101-117, and
+   its getters getGridDimensions / getCellSize / getCurrentFrame /
+   getNumMarkerParticles / getNumDiffuseParticles / getNumSolidCells /
+   isFluidBrickGridEnabled, fluidsimulationsavestate.h:47-67).  Any output
+   pointer may be NULL. */
+int gfs_savestate_read_header(const char *path, int *ni, int *nj, int *nk, double *dx,
+                              int *current_frame, int64_t *num_marker_particles,
+                              int64_t *num_diffuse_particles, int64_t *num_solid_cells,
+                              int *brick_grid);
+
+/* FluidSimulation::saveState (fluidsimulation.cpp:60-65 ->
+   FluidSimulationSaveState::saveState, fluidsimulationsavestate.cpp:31-99): the
+   simulation's marker particles (in the device's (cell, id) order) and solid
+   cells (i fastest) in the reference's file format, with current_frame in the
+   header, no diffuse particles and no brick grid.  The particles go from the
+   device to the file through pinned chunks; the call synchronises the stream. */
+int gfs_sim_save_state(gfs_sim *sim, const char *path, int current_frame);
+
+/* FluidSimulation(FluidSimulationSaveState&) (fluidsimulation.cpp:35-39,
+   _initializeSimulationFromSaveState :1638-1663): replace the simulation's
+   material grid by the file's solid cells (all other cells air) and its particles
+   by the file's marker particles (ids 0..n-1 in file order; particles in solid
+   cells are removed, as gfs_sim_set_particles does).  The grid dimensions and dx
+   must equal the simulation's; diffuse particles and brick grid data are skipped.
+   *current_frame (may be NULL) receives the header's frame.  Fails with
+   GFS_ERR_INVALID on a missing, truncated or mismatching file. */
+int gfs_sim_load_state(gfs_sim *sim, const char *path, int *current_frame);
+
 /* ------------------------------------------------ differentiable rollout */
 
 /* A differentiable rollout of `nsteps` substeps of length dt over n particles
