@@ -26,6 +26,8 @@ accuracy_vs_fp64  per timed substep (re-run untimed): max|p - p_ref| / max|p_ref
            residual max|b - A p| of the step's pressure, for both forms.
 savestate  FluidSimulationSaveState write / read of the whole state (GB/s), with the
            oracle's CPU writer beside it.
+fluid_sources  ms per _updateFluidSources call on the 256^3 state (inflow sphere,
+           outflow box).
 adjoint    fwd+adjoint ms/substep and peak HBM of the two differentiable
            configurations (32^3 cube, 20 substeps, MAC-field parameters; 128^3
            dam break, 60 substeps, per-particle velocities, Adam steps).
@@ -340,6 +342,33 @@ def savestate_bench(sim):
     return out
 
 
+def fluidsource_bench(sim):
+    """The fluid-source stage (_updateFluidSources) on the 256^3 state through
+    gfs_sim_update_fluid_sources: an inflow sphere of radius 12 cells in the air
+    region and an outflow box of 32 x 12 x 32 cells inside the slab.  First call:
+    the sphere's cells are filled (8 particles per air cell, then the empty
+    sub-cells); later calls find the sub-cells occupied.  Wall clock around each
+    call, which includes the re-sort of all particles after the change."""
+    from gridfluidsim3d_gb300 import CuboidFluidSource, SphericalFluidSource
+    dx = sim.dx
+    inflow = SphericalFluidSource((96 * dx, 200 * dx, 96 * dx), 12 * dx, (0.0, -2.0, 0.0))
+    outflow = CuboidFluidSource((160 * dx, 8 * dx, 160 * dx), 32 * dx, 12 * dx, 32 * dx)
+    outflow.is_inflow = False
+    sim.remove_fluid_sources()
+    sim.add_spherical_fluid_source(inflow)
+    sim.add_cuboid_fluid_source(outflow)
+    calls = []
+    for _ in range(3):
+        sim.ctx.synchronize()
+        t0 = time.perf_counter()
+        added, removed = sim.update_fluid_sources()
+        sim.ctx.synchronize()
+        calls.append({"ms": round((time.perf_counter() - t0) * 1e3, 3), "added": added, "removed": removed})
+    sim.remove_fluid_sources()
+    return {"particles_after": sim.get_num_marker_particles(), "calls": calls,
+            "note": "wall clock around gfs_sim_update_fluid_sources, including the re-sort"}
+
+
 def adjoint_bench(ctx, iters=2, warmup=1):
     """fwd+adjoint ms/step of the two differentiable configurations.
 
@@ -515,9 +544,10 @@ def main(args):
     ctx.synchronize()
     te = reduce_max(time.perf_counter() - t0, world)
 
-    savestate = None
+    savestate = sources = None
     if r == 0 and world == 1 and not args.no_savestate and set(forms) == {"plain", "mixed"}:
         savestate = savestate_bench(sim)
+        sources = fluidsource_bench(sim)
     adjoint = None
     if r == 0 and world == 1 and not args.no_adjoint and set(forms) == {"plain", "mixed"}:
         sim.close()
@@ -600,6 +630,7 @@ def main(args):
             "clocks": clocks,
             "adjoint": adjoint,
             "savestate": savestate,
+            "fluid_sources": sources,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -51,6 +51,12 @@ class StepStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class FluidSourceC(ctypes.Structure):
+    _fields_ = [("shape", ctypes.c_int), ("outflow", ctypes.c_int), ("active", ctypes.c_int),
+                ("position", ctypes.c_float * 3), ("radius", ctypes.c_double), ("size", ctypes.c_double * 3),
+                ("velocity", ctypes.c_float * 3)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _I64 = ctypes.c_int64
@@ -89,6 +95,9 @@ _SIGNATURES = {
     "gfs_sim_step": [_P, _D, ctypes.POINTER(StepStats)],
     "gfs_sim_step_host": [_P, _D, _P, _P, _P, ctypes.POINTER(_I64), ctypes.POINTER(StepStats)],
     "gfs_sim_pressure_check": [_P, _D, _D, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_I)],
+    "gfs_sim_set_fluid_sources": [_P, ctypes.POINTER(FluidSourceC), _I],
+    "gfs_sim_set_marker_particle_jitter": [_P, _D, ctypes.c_uint64],
+    "gfs_sim_update_fluid_sources": [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)],
     "gfs_savestate_read_header": [ctypes.c_char_p, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
                                   ctypes.POINTER(_D), ctypes.POINTER(_I), ctypes.POINTER(_I64),
                                   ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I)],

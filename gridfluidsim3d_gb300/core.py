@@ -433,6 +433,46 @@ class FluidSimulation:
         _lib.lib().gfs_sim_get_pressure_grid(self._h, _p(out))
         return out
 
+    # -- fluid sources (fluidsimulation.cpp:767-810; pyfluid/fluidsimulation.py:626-648) --
+    def _push_sources(self):
+        srcs = getattr(self, "_sources", [])
+        arr = (_lib.FluidSourceC * max(len(srcs), 1))()
+        for q, s in enumerate(srcs):
+            arr[q] = s._c()
+        _lib.lib().gfs_sim_set_fluid_sources(self._h, arr, len(srcs))
+
+    def add_spherical_fluid_source(self, source):
+        if not isinstance(source, SphericalFluidSource):
+            raise TypeError("source must be a SphericalFluidSource")
+        self._sources = getattr(self, "_sources", []) + [source]
+        self._push_sources()
+
+    def add_cuboid_fluid_source(self, source):
+        if not isinstance(source, CuboidFluidSource):
+            raise TypeError("source must be a CuboidFluidSource")
+        self._sources = getattr(self, "_sources", []) + [source]
+        self._push_sources()
+
+    def remove_fluid_source(self, source):
+        self._sources = [s for s in getattr(self, "_sources", []) if s is not source]
+        self._push_sources()
+
+    def remove_fluid_sources(self):
+        self._sources = []
+        self._push_sources()
+
+    def set_marker_particle_jitter(self, factor, seed=0):
+        """Jitter of source-added particles: 0.25 * factor * dx per component."""
+        _lib.lib().gfs_sim_set_marker_particle_jitter(self._h, float(factor), int(seed))
+
+    def update_fluid_sources(self):
+        """Apply the fluid sources once (re-reading their parameters); returns
+        (added, removed).  update() applies them at every step."""
+        self._push_sources()
+        a, r = ctypes.c_int64(), ctypes.c_int64()
+        _lib.lib().gfs_sim_update_fluid_sources(self._h, ctypes.byref(a), ctypes.byref(r))
+        return a.value, r.value
+
     # -- savestates (FluidSimulationSaveState file format) --
     def save_state(self, filename, current_frame=None):
         """FluidSimulation.save_state (pyfluid/fluidsimulation.py:109-113): the
@@ -467,6 +507,8 @@ class FluidSimulation:
         """One substep of length dt (FluidSimulation::update, fluidsimulation.cpp:3417-3455)."""
         if dt < 0.0:
             raise GFSError(_lib.GFS_ERR_INVALID, "update", f"delta time must be >= 0 (got {dt})")
+        if getattr(self, "_sources", None):
+            self._push_sources()          # sources are mutable objects, as in pyfluid
         st = StepStats()
         _lib.lib().gfs_sim_step(self._h, float(dt), ctypes.byref(st))
         self.last_stats = st.as_dict()
@@ -555,3 +597,59 @@ class FluidSimulationSaveState:
 
     def is_fluid_brick_grid_enabled(self):
         return self._hdr()["brick"]
+
+
+class FluidSource:
+    """FluidSource (fluidsource.h; pyfluid/fluidsource.py:10-123): position,
+    velocity, inflow/outflow and active state of a source."""
+
+    def __init__(self, position=(0.0, 0.0, 0.0), velocity=(0.0, 0.0, 0.0)):
+        self.position = tuple(float(x) for x in position)
+        self.velocity = tuple(float(x) for x in velocity)
+        self.is_inflow = True
+        self.is_active = True
+
+    @property
+    def is_outflow(self):
+        return not self.is_inflow
+
+    @is_outflow.setter
+    def is_outflow(self, value):
+        self.is_inflow = not bool(value)
+
+    def _c(self):
+        c = _lib.FluidSourceC()
+        c.outflow = 0 if self.is_inflow else 1
+        c.active = 1 if self.is_active else 0
+        c.position = (ctypes.c_float * 3)(*self.position)
+        c.velocity = (ctypes.c_float * 3)(*self.velocity)
+        return c
+
+
+class SphericalFluidSource(FluidSource):
+    """SphericalFluidSource(position, radius) (sphericalfluidsource.cpp:25-29)."""
+
+    def __init__(self, position=(0.0, 0.0, 0.0), radius=0.0, velocity=(0.0, 0.0, 0.0)):
+        super().__init__(position, velocity)
+        self.radius = float(radius)
+
+    def _c(self):
+        c = super()._c()
+        c.shape = 0
+        c.radius = self.radius
+        return c
+
+
+class CuboidFluidSource(FluidSource):
+    """CuboidFluidSource(position, width, height, depth) (cuboidfluidsource.cpp:25-41):
+    the box [position, position + (width, height, depth))."""
+
+    def __init__(self, position=(0.0, 0.0, 0.0), width=0.0, height=0.0, depth=0.0, velocity=(0.0, 0.0, 0.0)):
+        super().__init__(position, velocity)
+        self.width, self.height, self.depth = float(width), float(height), float(depth)
+
+    def _c(self):
+        c = super()._c()
+        c.shape = 1
+        c.size = (ctypes.c_double * 3)(self.width, self.height, self.depth)
+        return c

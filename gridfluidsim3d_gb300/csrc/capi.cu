@@ -263,6 +263,10 @@ static int sim_set_particles(Sim *s, const float *hp, const float *hv, const uin
     GFS_CUDA_CHECK(cudaMemcpyAsync(s->num.p, &hn, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     s->n_bound = n;
     s->need_sort = true;
+    // particles that fluid sources add take ids after every id given so far; with
+    // caller ids the maximum is found on the device when a source first needs it
+    s->next_id = (uint32_t)n;
+    s->next_id_valid = hid == nullptr;
     return GFS_OK;
 }
 
@@ -306,7 +310,13 @@ int sim_unstage_xyz(Sim *s, int64_t n) {
     GFS_CUDA_CHECK(cudaMemcpyAsync(s->num.p, &hn, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     s->n_bound = n;
     s->need_sort = true;
-    return sort_particles(s, true);
+    s->next_id = (uint32_t)n;
+    s->next_id_valid = true;
+    int rc = sort_particles(s, true);
+    if (rc) return rc;
+    // cells holding particles are fluid, as after the reference's initialisation
+    // (_initializeFluidMaterialParticlesFromSaveState, fluidsimulation.cpp:1466)
+    return classify_cells(s);
 }
 
 static int sim_get_particles(Sim *s, float *hp, float *hv, uint32_t *hid, int64_t *n_out) {
@@ -341,8 +351,13 @@ int sim_step(Sim *s, double dt, gfs_step_stats *stats) {
     }
     GFS_CUDA_CHECK(cudaEventRecord(s->ev0, st));
     int rc = GFS_OK;
-    // stage 1: _updateFluidCells (particle removal happened in the last sort)
+    // stage 1: _updateFluidCells (particle removal happened in the last sort), with
+    // the fluid sources first when there are any (fluidsimulation.cpp:1990-1994)
     if (s->need_sort && (rc = sort_particles(s, true))) return rc;
+    if (!s->sources.empty()) {
+        if ((rc = update_fluid_sources(s, nullptr, nullptr))) return rc;
+        if (s->need_sort && (rc = sort_particles(s, true))) return rc;
+    }
     if ((rc = classify_cells(s))) return rc;
     // stage 5: velocity splat, fill, saved field, body forces (stage 6 fused)
     if ((rc = splat_velocity(s))) return rc;
@@ -592,7 +607,11 @@ int gfs_sim_set_particles(gfs_sim *sim, const float *h_positions, const float *h
     GFS_NONNULL(sim);
     int rc = sim_set_particles(&sim->s, h_positions, h_velocities, h_ids, n);
     if (rc) return rc;
-    return sort_particles(&sim->s, true);
+    if ((rc = sort_particles(&sim->s, true))) return rc;
+    // cells holding particles are fluid, as after the reference's initialisation
+    // (FluidSimulation::_initializeFluidMaterial, fluidsimulation.cpp:1383), so that
+    // fluid sources see them as fluid
+    return classify_cells(&sim->s);
 }
 
 int gfs_sim_num_particles(gfs_sim *sim, int64_t *n) {

@@ -128,6 +128,12 @@ struct Sim {
     DevMem num;                  // uint32[4]: [0] particle count, [1] overflow flag
     DevMem pgrid;                // float pressure grid (unpadded) for get_pressure
     PressureWs ps;
+    std::vector<gfs_fluid_source> sources;   // FluidSimulation::_fluidSources
+    double jitter_factor = 0.1;              // _markerParticleJitterFactor (fluidsimulation.h:1111)
+    unsigned long long jitter_seed = 0;
+    uint32_t next_id = 0;                    // first id not yet given to a particle
+    bool next_id_valid = true;               // false: recompute from the particles' ids
+    DevMem src_mark, src_a, src_b, src_tmp;  // fluid-source work buffers
     gfs_step_stats last{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evp0 = nullptr, evp1 = nullptr;
 };
@@ -147,6 +153,9 @@ int face_fill(Sim *s, double dt);     // a3 + saved copy + body forces
 int sim_step(Sim *s, double dt, gfs_step_stats *stats);   // one device-resident substep
 int sim_stage_xyz(Sim *s, int64_t *n_out);   // particles -> xyz triples in pos_alt / vel_alt (ids in key)
 int sim_unstage_xyz(Sim *s, int64_t n);      // n staged triples (ids 0..n-1) -> particles, sorted
+
+// ---- sources.cu
+int update_fluid_sources(Sim *s, int64_t *added, int64_t *removed);   // _updateFluidSources
 
 // ---- adjoint.cu: the differentiable rollout
 struct DiffRun;

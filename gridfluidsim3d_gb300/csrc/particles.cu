@@ -49,8 +49,12 @@ __global__ void k_keys(const float4 *__restrict__ pos, const uint32_t *__restric
             j = (int)floor((double)x.y * invdx_d);
             k = (int)floor((double)x.z * invdx_d);
         }
-        if (c.in(i, j, k) && mat[c.at(i, j, k)] != GFS_SOLID)
-            kk = (uint32_t)i + (uint32_t)c.nx * ((uint32_t)j + (uint32_t)c.ny * (uint32_t)k);
+        // solid cells, and cells an outflow source flagged (bit 0x80), keep no particle
+        if (c.in(i, j, k)) {
+            const uint8_t m = mat[c.at(i, j, k)];
+            if (m != GFS_SOLID && !(m & 0x80))
+                kk = (uint32_t)i + (uint32_t)c.nx * ((uint32_t)j + (uint32_t)c.ny * (uint32_t)k);
+        }
     }
     key[p] = kk;
     if (kk != KEY_INVALID) slot[p] = atomicAdd(&count[kk], 1u);

@@ -239,6 +239,43 @@ int gfs_sim_step_host(gfs_sim *sim, double dt, float *h_positions, float *h_velo
 int gfs_sim_pressure_check(gfs_sim *sim, double dt, double rel_tol, double *fp64_residual,
                            double *rel_error, int *ref_iterations);
 
+/* ---------------------------------------------------------- fluid sources */
+
+/* A fluid source (FluidSource, fluidsource.h; SphericalFluidSource(vec3 position,
+   double radius), sphericalfluidsource.cpp:25-29; CuboidFluidSource(vec3 position,
+   double width, height, depth), cuboidfluidsource.cpp:25-41) as
+   FluidSimulation::addSphericalFluidSource / addCuboidFluidSource register it
+   (fluidsimulation.cpp:767-795). */
+#define GFS_SOURCE_SPHERE 0
+#define GFS_SOURCE_CUBOID 1
+typedef struct gfs_fluid_source {
+    int shape;             /* GFS_SOURCE_SPHERE or GFS_SOURCE_CUBOID                  */
+    int outflow;           /* 0: inflow (setAsInFlow, the default); 1: outflow        */
+    int active;            /* activate() / deactivate()                               */
+    float position[3];     /* sphere centre; cuboid minimum corner (vmath::vec3)      */
+    double radius;         /* sphere radius                                           */
+    double size[3];        /* cuboid width, height, depth                             */
+    float velocity[3];     /* setVelocity: velocity of the particles an inflow adds   */
+} gfs_fluid_source;
+
+/* Replace the simulation's fluid sources (copied; n = 0 removes them all).
+   While any is set, every gfs_sim_step applies them where the reference does, at
+   the start of _updateFluidCells (fluidsimulation.cpp:1990-1994), after the
+   particles in solid cells are removed: _updateFluidSources (:1854-1879). */
+int gfs_sim_set_fluid_sources(gfs_sim *sim, const gfs_fluid_source *sources, int n);
+
+/* Jitter of the particles sources add: each component in [-j, j],
+   j = 0.25 * factor * dx (FluidSimulation::_getMarkerParticleJitter,
+   fluidsimulation.cpp:1219-1221; factor 0.1 by default, fluidsimulation.h:1111).
+   The reference draws the jitter from rand(); here it is a counter-based hash of
+   (seed, particle id, axis), so runs are reproducible.  factor in [0, 1]; with 0
+   the positions are the reference's exactly. */
+int gfs_sim_set_marker_particle_jitter(gfs_sim *sim, double factor, uint64_t seed);
+
+/* Apply the fluid sources once, outside a step (the source stage of
+   _updateFluidCells alone), and sort the particles.  Outputs may be NULL. */
+int gfs_sim_update_fluid_sources(gfs_sim *sim, int64_t *num_added, int64_t *num_removed);
+
 /* ------------------------------------------------------------- savestates */
 
 /* The header of a FluidSimulationSaveState file

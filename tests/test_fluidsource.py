@@ -1,0 +1,61 @@
+"""Fluid sources (FluidSimulation::_updateFluidSources, fluidsimulation.cpp:1717-1879)
+on the CPU: the oracle's restatement against the result the reference's own
+code produced on the same state and sources (tests/golden/make_fluidsource_golden.py,
+jitter factor 0), and the jittered form's invariants.
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+from oracle import fluidsource as F  # noqa: E402
+from oracle import savestate as S  # noqa: E402
+
+G = os.path.join(HERE, "golden")
+
+
+def load_case():
+    inp = S.read_state(os.path.join(G, "fluidsource_in.state"))
+    ref = S.read_state(os.path.join(G, "fluidsource_ref.state"))
+    srcs = json.load(open(os.path.join(G, "fluidsource_sources.json")))
+    dims, dx = inp["dims"], inp["dx"]
+    mat = S.material_from_solid(dims, inp["solid_cells"])
+    g = np.floor(inp["positions"].astype(np.float64) / dx).astype(int)
+    # fluid where particles are, as the reference marks them after loading
+    # (_initializeFluidMaterialParticlesFromSaveState, fluidsimulation.cpp:1466)
+    mat[g[:, 2], g[:, 1], g[:, 0]] = F.FLUID
+    return inp, ref, srcs, mat
+
+
+def rows(p, v):
+    return np.sort(np.concatenate([p, v], 1).astype(np.float32).view([("", np.float32)] * 6).ravel())
+
+
+def test_oracle_matches_reference_sources():
+    inp, ref, srcs, mat = load_case()
+    _, p, v, ids, nid = F.update_fluid_sources(inp["dims"], inp["dx"], mat, inp["positions"], inp["velocities"],
+                                              np.arange(len(inp["positions"])), srcs, jitter_factor=0.0)
+    assert len(p) == len(ref["positions"]) == 5382
+    assert np.array_equal(rows(p, v), rows(ref["positions"], ref["velocities"]))
+    assert len(np.unique(ids)) == len(ids)
+
+
+def test_jittered_particles_stay_in_their_sub_cells():
+    inp, _, srcs, mat = load_case()
+    n0 = len(inp["positions"])
+    _, p0, _, i0, _ = F.update_fluid_sources(inp["dims"], inp["dx"], mat, inp["positions"], inp["velocities"],
+                                            np.arange(n0), srcs, jitter_factor=0.0)
+    _, p1, v1, i1, _ = F.update_fluid_sources(inp["dims"], inp["dx"], mat, inp["positions"], inp["velocities"],
+                                             np.arange(n0), srcs, jitter_factor=0.1, seed=5)
+    assert np.array_equal(i0, i1)
+    new = i1 >= n0
+    d = np.abs(p1[new].astype(np.float64) - p0[new])
+    # the default factor 0.1: |jitter| <= 0.025 dx, well inside a sub-cell (half-width 0.25 dx),
+    # so the same sub-cells are filled and the ids match
+    jmax = 0.25 * 0.1 * inp["dx"]
+    assert d.max() <= jmax * (1 + 1e-6) and d.max() > 0.5 * jmax
+    assert np.array_equal(p1[~new], p0[~new])

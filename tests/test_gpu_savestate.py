@@ -4,7 +4,8 @@ oracle's restatement of the FluidSimulationSaveState format and the fixture the
 reference's own FluidSimulation wrote (tests/golden/savestate_ref.state).
 
 Bars: the file's particles and solid cells arrive bit for bit (particles by id =
-position in the file); a written file is byte-identical to the oracle's file of
+position in the file; cells holding particles become fluid, as after the
+reference's load); a written file is byte-identical to the oracle's file of
 the simulation's own state (particles in its (cell, id) order); load after save
 reproduces the state; a substep after loading equals a substep after setting the
 same arrays directly.
@@ -33,8 +34,12 @@ def test_load_reference_fixture(gpu_ctx):
     sim = FluidSimulation.from_save_state(FREF, ctx=gpu_ctx)
     assert (sim.isize, sim.jsize, sim.ksize, sim.dx) == (*ref["dims"], ref["dx"])
     assert sim.current_frame == ref["frame"]
-    mat = sim.get_material_grid()
-    assert np.array_equal(mat, S.material_from_solid(ref["dims"], ref["solid_cells"]))
+    # the file's solid cells; cells holding particles are fluid, as the reference marks
+    # them after loading (_initializeFluidMaterialParticlesFromSaveState)
+    want = S.material_from_solid(ref["dims"], ref["solid_cells"])
+    g = np.floor(ref["positions"].astype(np.float64) / ref["dx"]).astype(int)
+    want[g[:, 2], g[:, 1], g[:, 0]] = 1
+    assert np.array_equal(sim.get_material_grid(), want)
     pos, vel, ids = _by_id(*sim.get_marker_particles())
     assert np.array_equal(ids, np.arange(len(ref["positions"]), dtype=np.uint32))
     assert np.array_equal(pos, ref["positions"]) and np.array_equal(vel, ref["velocities"])
@@ -68,9 +73,9 @@ def test_round_trip_and_step(gpu_ctx, tmp_path):
     pos, vel, _ = a.get_marker_particles()
     b = FluidSimulation(*sc.dims, sc.dx, max_particles=sc.num_particles, ctx=gpu_ctx)
     assert b.load_state(path) == 3
-    # a savestate holds the solid cells; every other cell comes back as air
+    # a savestate holds the solid cells; the others come back as air, or fluid where particles are
     ma, mb = a.get_material_grid(), b.get_material_grid()
-    assert np.array_equal(mb == S.SOLID, ma == S.SOLID) and np.all((mb == S.SOLID) | (mb == 0))
+    assert np.array_equal(mb == S.SOLID, ma == S.SOLID) and np.all(mb <= S.SOLID)
     bp, bv, bi = _by_id(*b.get_marker_particles())
     assert np.array_equal(bp, pos) and np.array_equal(bv, vel)
     # the loaded state steps exactly like the same arrays set directly
