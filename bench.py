@@ -369,6 +369,64 @@ def fluidsource_bench(sim):
             "note": "wall clock around gfs_sim_update_fluid_sources, including the re-sort"}
 
 
+def next_rows_bench(ctx, sim, sample=200_000, seed=0):
+    """The two callers beside the substep that reuse its kernels, through their
+    drop-in APIs with host buffers (copies inside the timed call), on the 256^3
+    state, each with the oracle (single thread) on a bounded sample beside it:
+
+    surface_splat   IsotropicParticleMesher's scalar field: CLScalarField::addPoints
+                    of every marker particle onto the (n+1)^3 node grid at dx,
+                    radius = marker particle radius x 3 (fluidsimulation.cpp:1401-1405,
+                    2051), threshold 1.0 (isotropicparticlemesher.h:112).
+    diffuse_rk2     DiffuseParticleSimulation's advection: ParticleAdvector::
+                    advectParticlesRK2 of 4M points (marker positions) through the
+                    simulation's MAC field, dt = 1/30."""
+    import oracle as O
+    from gridfluidsim3d_gb300 import CLScalarField, ParticleAdvector
+    rng = np.random.default_rng(seed)
+    pos, _, _ = sim.get_marker_particles()
+    dims, dx = (sim.isize, sim.jsize, sim.ksize), sim.dx
+    out = {}
+    # surface splat
+    r = (3 * dx ** 3 / 8.0 / (4 * 3.141592653)) ** (1.0 / 3.0) * 3.0
+    field = np.zeros((dims[2] + 1, dims[1] + 1, dims[0] + 1), np.float32)
+    acc = CLScalarField(ctx)
+    acc.set_max_scalar_field_value_threshold(1.0)
+    acc.add_points(pos[:1000], r, (0.0, 0.0, 0.0), dx, field)   # warm-up
+    field[:] = 0
+    t0 = time.perf_counter()
+    acc.add_points(pos, r, (0.0, 0.0, 0.0), dx, field)
+    t_gpu = time.perf_counter() - t0
+    sel = pos[rng.choice(len(pos), sample, replace=False)]
+    t0 = time.perf_counter()
+    O.splat_points(sel, None, r, (0.0, 0.0, 0.0), dx, np.zeros_like(field), threshold=1.0)
+    t_cpu = (time.perf_counter() - t0) * len(pos) / sample
+    out["surface_splat"] = {"points": int(len(pos)), "radius_cells": round(r / dx, 4), "gpu_s": round(t_gpu, 4),
+                            "gpu_mpoints_s": round(len(pos) / t_gpu / 1e6, 1),
+                            "cpu_s_estimate": round(t_cpu, 1),
+                            "cpu_sample": f"oracle single thread on {sample} points, scaled"}
+    # diffuse-particle advection
+    f = sim.get_velocity_field()
+    pts = pos[rng.choice(len(pos), 4_000_000, replace=False)]
+    adv = ParticleAdvector(ctx)
+    adv.advect_particles_rk2(pts[:1000], f, 1.0 / 30.0)
+    t0 = time.perf_counter()
+    adv.advect_particles_rk2(pts, f, 1.0 / 30.0)
+    t_gpu = time.perf_counter() - t0
+    sel = pts[:sample]
+    t0 = time.perf_counter()
+    k1 = O.evaluate_velocity(dims, dx, f.u, f.v, f.w, sel)
+    mid = (sel + np.float32(0.5 / 30.0) * k1).astype(np.float32)
+    k2 = O.evaluate_velocity(dims, dx, f.u, f.v, f.w, mid)
+    _ = (sel + np.float32(1.0 / 30.0) * k2).astype(np.float32)
+    t_cpu = (time.perf_counter() - t0) * len(pts) / sample
+    out["diffuse_rk2"] = {"points": int(len(pts)), "gpu_s": round(t_gpu, 4),
+                          "gpu_mpoints_s": round(len(pts) / t_gpu / 1e6, 1), "cpu_s_estimate": round(t_cpu, 1),
+                          "cpu_sample": f"oracle single thread on {sample} points, scaled"}
+    out["note"] = "wall clock around each drop-in call, host arrays in and out"
+    return out
+
+
 def adjoint_bench(ctx, iters=2, warmup=1):
     """fwd+adjoint ms/step of the two differentiable configurations.
 
@@ -544,10 +602,11 @@ def main(args):
     ctx.synchronize()
     te = reduce_max(time.perf_counter() - t0, world)
 
-    savestate = sources = None
+    savestate = sources = next_rows = None
     if r == 0 and world == 1 and not args.no_savestate and set(forms) == {"plain", "mixed"}:
         savestate = savestate_bench(sim)
         sources = fluidsource_bench(sim)
+        next_rows = next_rows_bench(ctx, sim)
     adjoint = None
     if r == 0 and world == 1 and not args.no_adjoint and set(forms) == {"plain", "mixed"}:
         sim.close()
@@ -631,6 +690,7 @@ def main(args):
             "adjoint": adjoint,
             "savestate": savestate,
             "fluid_sources": sources,
+            "surface_splat_and_diffuse_advection": next_rows,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -20,7 +20,7 @@
 //
 // Geometry follows the reference's types step by step: positions are
 // vmath::vec3 (float), radii, extents and dx double, index bounds from
-// Grid3d::getGridIndexBounds / fitAABBtoGrid (grid3d.h:350-420), the overlap
+// Grid3d::getGridIndexBounds / fitAABBtoGrid (grid3d.h:350-371, 426-439, 485-502), the overlap
 // test a float dot product compared with a double radius squared.  The box
 // bounds are computed on the host; the per-cell tests run on the device with
 // non-contracted float arithmetic.
@@ -79,7 +79,7 @@ struct Box {
     double w[3];
 };
 
-// Grid3d::getGridIndexBounds(AABB, ...) (:384-397)
+// Grid3d::getGridIndexBounds(AABB, ...) (:426-439)
 void bounds_box(const Box &b, double dx, int ni, int nj, int nk, I3 &g1, I3 &g2) {
     float q[3] = {b.p[0] + (float)b.w[0], b.p[1] + (float)b.w[1], b.p[2] + (float)b.w[2]};
     g1 = pos_to_index(b.p[0], b.p[1], b.p[2], dx);
@@ -88,7 +88,7 @@ void bounds_box(const Box &b, double dx, int ni, int nj, int nk, I3 &g1, I3 &g2)
     g2 = {(int)fmin(g2.i, ni - 1), (int)fmin(g2.j, nj - 1), (int)fmin(g2.k, nk - 1)};
 }
 
-// Grid3d::fitAABBtoGrid (:404-420) and AABB(vec3 p1, vec3 p2) (aabb.cpp:33-45)
+// Grid3d::fitAABBtoGrid (:485-502) and AABB(vec3 p1, vec3 p2) (aabb.cpp:33-45)
 Box fit_box(const Box &b, double dx, int ni, int nj, int nk) {
     float pmin[3] = {b.p[0], b.p[1], b.p[2]};
     float pmax[3] = {b.p[0] + (float)b.w[0], b.p[1] + (float)b.w[1], b.p[2] + (float)b.w[2]};
