@@ -83,7 +83,7 @@ struct PsCtrl {
     int refinements;
     unsigned err;                // GFS_DEV_ERR_* bits
     unsigned tickets[4];         // last-block-done tickets of fused reductions
-    unsigned sweep_ticket[3];    // dispatch tickets of the wavefront kernels (fwd, bwd, precon)
+    unsigned sweep_ticket[3];    // dispatch tickets of the wavefront kernels, by kind (precon, fwd, bwd)
     unsigned epoch;              // tag of the current wavefront's exchange words
 };
 
