@@ -98,6 +98,8 @@ _SIGNATURES = {
     "gfs_sim_set_fluid_sources": [_P, ctypes.POINTER(FluidSourceC), _I],
     "gfs_sim_set_marker_particle_jitter": [_P, _D, ctypes.c_uint64],
     "gfs_sim_update_fluid_sources": [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)],
+    "gfs_sim_add_fluid_cells": [_P, _P, _I, _P],
+    "gfs_sim_remove_fluid_cells": [_P, _P, _I],
     "gfs_savestate_read_header": [ctypes.c_char_p, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
                                   ctypes.POINTER(_D), ctypes.POINTER(_I), ctypes.POINTER(_I64),
                                   ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I)],

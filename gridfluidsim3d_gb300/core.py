@@ -316,8 +316,9 @@ class FluidSimulation:
     """Device-resident FLIP simulation behind a subset of pyfluid's FluidSimulation.
 
     ``update(dt)`` runs one substep of length dt (stages 1, 5-9, 11, 12 of
-    FluidSimulation::_stepFluid); meshing, level set, diffuse particles, fluid
-    sources and autosave are not part of this core.
+    FluidSimulation::_stepFluid), with the queued fluid cells and the fluid
+    sources at its start; meshing, level set, diffuse particles and autosave are
+    not part of this core.
     """
 
     def __init__(self, isize, jsize, ksize, dx, max_particles, ctx: Context | None = None):
@@ -466,12 +467,33 @@ class FluidSimulation:
         _lib.lib().gfs_sim_set_marker_particle_jitter(self._h, float(factor), int(seed))
 
     def update_fluid_sources(self):
-        """Apply the fluid sources once (re-reading their parameters); returns
-        (added, removed).  update() applies them at every step."""
+        """Apply the queued fluid cells and the fluid sources once (re-reading
+        the sources' parameters); returns (added, removed).  update() applies
+        them at every step."""
         self._push_sources()
         a, r = ctypes.c_int64(), ctypes.c_int64()
         _lib.lib().gfs_sim_update_fluid_sources(self._h, ctypes.byref(a), ctypes.byref(r))
         return a.value, r.value
+
+    # -- fluid-cell queues (fluidsimulation.cpp:887-940; pyfluid/fluidsimulation.py:673-700) --
+    @staticmethod
+    def _cells(cell_list):
+        """cell_list: objects with .i/.j/.k (pyfluid's GridIndex) or (i, j, k) rows."""
+        if len(cell_list) and hasattr(cell_list[0], "i"):
+            cell_list = [(c.i, c.j, c.k) for c in cell_list]
+        return np.ascontiguousarray(np.asarray(cell_list, np.int32).reshape(-1, 3))
+
+    def add_fluid_cells(self, cell_list, vx=0.0, vy=0.0, vz=0.0):
+        """Queue cells to become fluid at the next update, 8 particles each with
+        velocity (vx, vy, vz); only cells that are air now are queued."""
+        c = self._cells(cell_list)
+        v = (ctypes.c_float * 3)(vx, vy, vz)
+        _lib.lib().gfs_sim_add_fluid_cells(self._h, _p(c), len(c), v)
+
+    def remove_fluid_cells(self, cell_list):
+        """Queue cells whose marker particles the next update removes."""
+        c = self._cells(cell_list)
+        _lib.lib().gfs_sim_remove_fluid_cells(self._h, _p(c), len(c))
 
     # -- savestates (FluidSimulationSaveState file format) --
     def save_state(self, filename, current_frame=None):

@@ -352,12 +352,16 @@ int sim_step(Sim *s, double dt, gfs_step_stats *stats) {
     GFS_CUDA_CHECK(cudaEventRecord(s->ev0, st));
     int rc = GFS_OK;
     // stage 1: _updateFluidCells (particle removal happened in the last sort), with
-    // the fluid sources first when there are any (fluidsimulation.cpp:1990-1994)
+    // the queued fluid cells and the fluid sources first when there are any
+    // (fluidsimulation.cpp:1990-1994)
     if (s->need_sort && (rc = sort_particles(s, true))) return rc;
+    if (!s->added_cells.empty() || !s->removed_cells.empty()) {
+        if ((rc = update_fluid_cell_queues(s, nullptr, nullptr))) return rc;
+    }
     if (!s->sources.empty()) {
         if ((rc = update_fluid_sources(s, nullptr, nullptr))) return rc;
-        if (s->need_sort && (rc = sort_particles(s, true))) return rc;
     }
+    if (s->need_sort && (rc = sort_particles(s, true))) return rc;
     if ((rc = classify_cells(s))) return rc;
     // stage 5: velocity splat, fill, saved field, body forces (stage 6 fused)
     if ((rc = splat_velocity(s))) return rc;

@@ -134,6 +134,14 @@ struct Sim {
     uint32_t next_id = 0;                    // first id not yet given to a particle
     bool next_id_valid = true;               // false: recompute from the particles' ids
     DevMem src_mark, src_a, src_b, src_tmp;  // fluid-source work buffers
+    // FluidSimulation::_addedFluidCellQueue / _removedFluidCellQueue
+    // (fluidsimulation.h:1108-1109): cell triples (i, j, k), applied at the next step
+    struct CellGroup {
+        std::vector<int32_t> ijk;
+        float vel[3];
+    };
+    std::vector<CellGroup> added_cells;
+    std::vector<int32_t> removed_cells;
     gfs_step_stats last{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evp0 = nullptr, evp1 = nullptr;
 };
@@ -156,6 +164,8 @@ int sim_unstage_xyz(Sim *s, int64_t n);      // n staged triples (ids 0..n-1) ->
 
 // ---- sources.cu
 int update_fluid_sources(Sim *s, int64_t *added, int64_t *removed);   // _updateFluidSources
+// _updateAddedFluidCellQueue + _updateRemovedFluidCellQueue
+int update_fluid_cell_queues(Sim *s, int64_t *added, int64_t *removed);
 
 // ---- adjoint.cu: the differentiable rollout
 struct DiffRun;

@@ -49,7 +49,8 @@ __global__ void k_keys(const float4 *__restrict__ pos, const uint32_t *__restric
             j = (int)floor((double)x.y * invdx_d);
             k = (int)floor((double)x.z * invdx_d);
         }
-        // solid cells, and cells an outflow source flagged (bit 0x80), keep no particle
+        // solid cells, and cells flagged by an outflow source or the removed-cell
+        // queue (bit 0x80), keep no particle
         if (c.in(i, j, k)) {
             const uint8_t m = mat[c.at(i, j, k)];
             if (m != GFS_SOLID && !(m & 0x80))

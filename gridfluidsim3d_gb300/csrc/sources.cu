@@ -34,6 +34,7 @@
 // the reference creates them (cells, then sub-cells, each i fastest).
 #include <cmath>
 #include <cstdint>
+#include <unordered_set>
 #include <vector>
 
 #include "gfs_internal.h"
@@ -213,7 +214,30 @@ __global__ void k_src_cells(SrcGeom G, GridDim c, double dx, const uint8_t *__re
     is_air[li] = t == 1;
 }
 
-// 1'. 8 particles per air cell (_addMarkerParticlesToCell point order), the cell becomes fluid
+// _addMarkerParticlesToCell (:1223-1246): 8 particles at the cell's 2x2x2
+// sub-cell centres plus jitter, written to slots slot0.. with ids id0..
+__device__ __forceinline__ void add_cell_particles(int i, int j, int k, double dx, const float v[3],
+                                                   float4 *__restrict__ pos, float4 *__restrict__ vel,
+                                                   long long slot0, uint32_t id0, unsigned long long seed,
+                                                   double jit) {
+    const double q = 0.25 * dx;
+    const float cx = cell_center(i, dx), cy = cell_center(j, dx), cz = cell_center(k, dx);
+    // (-,-,-) (+,-,-) (+,-,+) (-,-,+) (-,+,-) (+,+,-) (+,+,+) (-,+,+)
+    const int sx[8] = {-1, 1, 1, -1, -1, 1, 1, -1}, sy[8] = {-1, -1, -1, -1, 1, 1, 1, 1},
+              sz[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+    for (int idx = 0; idx < 8; idx++) {
+        uint32_t id = id0 + (uint32_t)idx;
+        float px = (float)((double)cx + sx[idx] * q), py = (float)((double)cy + sy[idx] * q),
+              pz = (float)((double)cz + sz[idx] * q);
+        px = __fadd_rn(px, jitter_component(seed, id, 0, jit));
+        py = __fadd_rn(py, jitter_component(seed, id, 1, jit));
+        pz = __fadd_rn(pz, jitter_component(seed, id, 2, jit));
+        pos[slot0 + idx] = make_float4(px, py, pz, __uint_as_float(id));
+        vel[slot0 + idx] = make_float4(v[0], v[1], v[2], 0.f);
+    }
+}
+
+// 1'. 8 particles per air cell, the cell becomes fluid
 __global__ void k_src_fill_cells(SrcGeom G, GridDim c, double dx, uint8_t *__restrict__ mat,
                                  const uint8_t *__restrict__ mark, const uint32_t *__restrict__ scan, long long n,
                                  float4 *__restrict__ pos, float4 *__restrict__ vel, long long base,
@@ -224,22 +248,8 @@ __global__ void k_src_fill_cells(SrcGeom G, GridDim c, double dx, uint8_t *__res
     box_index(li, G.n1, x, y, z);
     int i = G.g1[0] + x, j = G.g1[1] + y, k = G.g1[2] + z;
     mat[c.at(i, j, k)] = GFS_FLUID;
-    const double q = 0.25 * dx;
-    const float cx = cell_center(i, dx), cy = cell_center(j, dx), cz = cell_center(k, dx);
-    // (-,-,-) (+,-,-) (+,-,+) (-,-,+) (-,+,-) (+,+,-) (+,+,+) (-,+,+)
-    const int sx[8] = {-1, 1, 1, -1, -1, 1, 1, -1}, sy[8] = {-1, -1, -1, -1, 1, 1, 1, 1},
-              sz[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
-    for (int idx = 0; idx < 8; idx++) {
-        long long q8 = (long long)scan[li] * 8 + idx;
-        uint32_t id = id0 + (uint32_t)q8;
-        float px = (float)((double)cx + sx[idx] * q), py = (float)((double)cy + sy[idx] * q),
-              pz = (float)((double)cz + sz[idx] * q);
-        px = __fadd_rn(px, jitter_component(seed, id, 0, jit));
-        py = __fadd_rn(py, jitter_component(seed, id, 1, jit));
-        pz = __fadd_rn(pz, jitter_component(seed, id, 2, jit));
-        pos[base + q8] = make_float4(px, py, pz, __uint_as_float(id));
-        vel[base + q8] = make_float4(G.vel[0], G.vel[1], G.vel[2], 0.f);
-    }
+    long long q8 = (long long)scan[li] * 8;
+    add_cell_particles(i, j, k, dx, G.vel, pos, vel, base + q8, id0 + (uint32_t)q8, seed, jit);
 }
 
 // 2. sub-cell grid of the fitted AABB: 1 for the sub-cells of overlapping fluid-or-air cells
@@ -327,6 +337,48 @@ __global__ void k_src_clear_flags(uint8_t *__restrict__ mat, long long n) {
     if (q < n) mat[q] &= (uint8_t)~GFS_REMOVE_FLAG;
 }
 
+// ---- fluid-cell queues (FluidSimulation::addFluidCells / removeFluidCells) ----
+
+// One queued cell of _addedFluidCellQueue with its group's velocity.
+struct CellEntry {
+    int i, j, k;
+    float v[3];
+};
+
+// addFluidCells keeps only the cells that are air when it is called (:900-902)
+__global__ void k_cells_material(GridDim c, const uint8_t *__restrict__ mat, const int32_t *__restrict__ ijk,
+                                 long long n, uint8_t *__restrict__ out) {
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q < n) out[q] = mat[c.at(ijk[3 * q], ijk[3 * q + 1], ijk[3 * q + 2])];
+}
+
+// _addNewFluidCells (:1749-1759): the entries whose cell is still air
+__global__ void k_cells_air(GridDim c, const uint8_t *__restrict__ mat, const CellEntry *__restrict__ e,
+                            long long n, uint32_t *__restrict__ is_air) {
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q < n) is_air[q] = mat[c.at(e[q].i, e[q].j, e[q].k)] == GFS_AIR;
+}
+
+// ... get 8 particles each and become fluid
+__global__ void k_cells_fill(GridDim c, double dx, uint8_t *__restrict__ mat, const CellEntry *__restrict__ e,
+                             const uint32_t *__restrict__ is_air, const uint32_t *__restrict__ scan, long long n,
+                             float4 *__restrict__ pos, float4 *__restrict__ vel, long long base, uint32_t id0,
+                             unsigned long long seed, double jit) {
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= n || !is_air[q]) return;
+    const CellEntry E = e[q];
+    mat[c.at(E.i, E.j, E.k)] = GFS_FLUID;
+    long long q8 = (long long)scan[q] * 8;
+    add_cell_particles(E.i, E.j, E.k, dx, E.v, pos, vel, base + q8, id0 + (uint32_t)q8, seed, jit);
+}
+
+// _updateRemovedFluidCellQueue (:1895-1930): the listed cells lose their particles at a sort
+__global__ void k_cells_mark_removal(GridDim c, uint8_t *__restrict__ mat, const int32_t *__restrict__ ijk,
+                                     long long n) {
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q < n) mat[c.at(ijk[3 * q], ijk[3 * q + 1], ijk[3 * q + 2])] |= GFS_REMOVE_FLAG;
+}
+
 // ---- driver ------------------------------------------------------------------
 
 namespace {
@@ -342,9 +394,31 @@ int scan_into(Ctx *ctx, Sim *s, uint32_t *in, uint32_t *out, long long n, uint32
     return GFS_OK;
 }
 
-int capacity_check(Sim *s, long long n, long long add) {
+// New particles take ids after every id given so far; after caller-chosen ids
+// that is the largest id + 1, found on the device once.
+int ensure_next_id(Sim *s, long long n) {
+    if (s->next_id_valid) return GFS_OK;
+    Ctx *ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    const int T = 256;
+    if (s->src_a.ensure(sizeof(uint32_t))) return GFS_ERR_NOMEM;
+    GFS_CUDA_CHECK(cudaMemsetAsync(s->src_a.p, 0, sizeof(uint32_t), st));
+    if (n > 0) {
+        k_src_max_id<<<grid_blocks(n, T), T, 0, st>>>(s->pos.as<float4>(), n, s->src_a.as<uint32_t>());
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+    }
+    uint32_t mx = 0;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(&mx, s->src_a.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GFS_CUDA_CHECK(cudaStreamSynchronize(st));
+    s->next_id = mx > s->next_id ? mx : s->next_id;
+    s->next_id_valid = true;
+    return GFS_OK;
+}
+
+int capacity_check(Sim *s, long long n, long long add, const char *what = "fluid sources") {
     if (n + add > s->capacity) {
-        set_error(GFS_ERR_INVALID, "fluid sources: %lld particles exceed the simulation's capacity %lld",
+        set_error(GFS_ERR_INVALID, "%s: %lld particles exceed the simulation's capacity %lld", what,
                   n + add, (long long)s->capacity);
         return GFS_ERR_INVALID;
     }
@@ -369,20 +443,7 @@ int update_fluid_sources(Sim *s, int64_t *added, int64_t *removed) {
     GFS_CUDA_CHECK(cudaMemcpyAsync(&hn, s->num.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     GFS_CUDA_CHECK(cudaStreamSynchronize(st));
     long long n = hn, n0 = hn;
-    if (!s->next_id_valid) {
-        if (s->src_a.ensure(sizeof(uint32_t))) return GFS_ERR_NOMEM;
-        GFS_CUDA_CHECK(cudaMemsetAsync(s->src_a.p, 0, sizeof(uint32_t), st));
-        if (n > 0) {
-            k_src_max_id<<<grid_blocks(n, T), T, 0, st>>>(s->pos.as<float4>(), n, s->src_a.as<uint32_t>());
-            ctx->launches++;
-            GFS_LAUNCH_CHECK();
-        }
-        uint32_t mx = 0;
-        GFS_CUDA_CHECK(cudaMemcpyAsync(&mx, s->src_a.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-        GFS_CUDA_CHECK(cudaStreamSynchronize(st));
-        s->next_id = mx > s->next_id ? mx : s->next_id;
-        s->next_id_valid = true;
-    }
+    if ((rc = ensure_next_id(s, n))) return rc;
     const double jit = 0.25 * s->jitter_factor * dx;
     uint8_t *mat = s->mat.as<uint8_t>();
     bool any_outflow = false;
@@ -466,6 +527,88 @@ int update_fluid_sources(Sim *s, int64_t *added, int64_t *removed) {
     return GFS_OK;
 }
 
+// The fluid-cell queues on the device state, as _updateFluidCells applies them
+// before the sources (fluidsimulation.cpp:1990-1993): every queued added cell
+// that is still air gets 8 particles with its group's velocity and becomes
+// fluid, groups and cells in the order they were queued (a cell queued twice
+// is fluid the second time); then the particles in the queued removed cells,
+// new ones included, are removed (the material is left as it is).  On an
+// error nothing is added and the queues are kept.
+int update_fluid_cell_queues(Sim *s, int64_t *added, int64_t *removed) {
+    Ctx *ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    const Grids &g = s->g;
+    const int T = 256;
+    if (added) *added = 0;
+    if (removed) *removed = 0;
+    if (s->added_cells.empty() && s->removed_cells.empty()) return GFS_OK;
+    int rc = GFS_OK;
+    uint32_t hn = 0;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(&hn, s->num.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GFS_CUDA_CHECK(cudaStreamSynchronize(st));
+    long long n = hn, n0 = hn;
+    uint8_t *mat = s->mat.as<uint8_t>();
+    if (!s->added_cells.empty()) {
+        std::vector<CellEntry> ent;
+        std::unordered_set<long long> seen;
+        for (const Sim::CellGroup &grp : s->added_cells)
+            for (size_t q = 0; q + 2 < grp.ijk.size(); q += 3) {
+                CellEntry e{grp.ijk[q], grp.ijk[q + 1], grp.ijk[q + 2], {grp.vel[0], grp.vel[1], grp.vel[2]}};
+                if (seen.insert(g.c.at(e.i, e.j, e.k)).second) ent.push_back(e);
+            }
+        long long m = (long long)ent.size();
+        if ((rc = ensure_next_id(s, n))) return rc;
+        if (s->src_mark.ensure((size_t)m * sizeof(CellEntry)) || s->src_a.ensure((size_t)(m + 1) * sizeof(uint32_t)) ||
+            s->src_b.ensure((size_t)(m + 1) * sizeof(uint32_t)))
+            return GFS_ERR_NOMEM;
+        const CellEntry *E = s->src_mark.as<CellEntry>();
+        uint32_t *a = s->src_a.as<uint32_t>(), *b = s->src_b.as<uint32_t>();
+        GFS_CUDA_CHECK(cudaMemcpyAsync(s->src_mark.p, ent.data(), (size_t)m * sizeof(CellEntry),
+                                       cudaMemcpyHostToDevice, st));
+        k_cells_air<<<grid_blocks(m, T), T, 0, st>>>(g.c, mat, E, m, a);
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+        uint32_t nair = 0;
+        if ((rc = scan_into(ctx, s, a, b, m, &nair))) return rc;
+        if ((rc = capacity_check(s, n, 8LL * nair, "added fluid cells"))) return rc;
+        if (nair > 0) {
+            k_cells_fill<<<grid_blocks(m, T), T, 0, st>>>(g.c, g.dx, mat, E, a, b, m, s->pos.as<float4>(),
+                                                          s->vel.as<float4>(), n, s->next_id, s->jitter_seed,
+                                                          0.25 * s->jitter_factor * g.dx);
+            ctx->launches++;
+            GFS_LAUNCH_CHECK();
+            n += 8LL * nair;
+            s->next_id += 8u * nair;
+            uint32_t hn2 = (uint32_t)n;
+            GFS_CUDA_CHECK(cudaMemcpyAsync(s->num.p, &hn2, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+            GFS_CUDA_CHECK(cudaStreamSynchronize(st));
+            s->n_bound = n;
+            s->need_sort = true;
+        }
+        s->added_cells.clear();
+        s->added_cells.shrink_to_fit();
+    }
+    if (added) *added = n - n0;
+    if (!s->removed_cells.empty()) {
+        long long m = (long long)s->removed_cells.size() / 3;
+        if (s->src_mark.ensure((size_t)m * 3 * sizeof(int32_t))) return GFS_ERR_NOMEM;
+        GFS_CUDA_CHECK(cudaMemcpyAsync(s->src_mark.p, s->removed_cells.data(), (size_t)m * 3 * sizeof(int32_t),
+                                       cudaMemcpyHostToDevice, st));
+        k_cells_mark_removal<<<grid_blocks(m, T), T, 0, st>>>(g.c, mat, s->src_mark.as<int32_t>(), m);
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+        if ((rc = sort_particles(s, true))) return rc;
+        k_src_clear_flags<<<grid_blocks(g.c.size, T), T, 0, st>>>(mat, g.c.size);
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+        GFS_CUDA_CHECK(cudaStreamSynchronize(st));
+        if (removed) *removed = n - s->n_bound;
+        s->removed_cells.clear();
+        s->removed_cells.shrink_to_fit();
+    }
+    return GFS_OK;
+}
+
 }  // namespace gfs
 
 using namespace gfs;
@@ -509,9 +652,66 @@ int gfs_sim_update_fluid_sources(gfs_sim *sim, int64_t *num_added, int64_t *num_
         set_error(GFS_ERR_INVALID, "sim must not be NULL");
         return GFS_ERR_INVALID;
     }
-    int rc = update_fluid_sources(&sim->s, num_added, num_removed);
-    if (rc) return rc;
-    if (sim->s.need_sort) return sort_particles(&sim->s, true);
+    Sim *s = &sim->s;
+    int64_t qa = 0, qr = 0, sa = 0, sr = 0;
+    int rc = GFS_OK;
+    if (s->need_sort && (rc = sort_particles(s, true))) return rc;
+    if ((rc = update_fluid_cell_queues(s, &qa, &qr))) return rc;
+    if ((rc = update_fluid_sources(s, &sa, &sr))) return rc;
+    if (num_added) *num_added = qa + sa;
+    if (num_removed) *num_removed = qr + sr;
+    if (s->need_sort) return sort_particles(s, true);
+    return GFS_OK;
+}
+
+namespace {
+int check_cells(const char *fn, const gfs_sim *sim, const int32_t *ijk, int n) {
+    if (!sim || n < 0 || (n > 0 && !ijk)) {
+        set_error(GFS_ERR_INVALID, "%s: invalid arguments", fn);
+        return GFS_ERR_INVALID;
+    }
+    const Grids &g = sim->s.g;
+    for (int q = 0; q < n; q++) {
+        // FluidSimulation::addFluidCells / removeFluidCells throw std::out_of_range
+        if (!g.c.in(ijk[3 * q], ijk[3 * q + 1], ijk[3 * q + 2])) {
+            set_error(GFS_ERR_INVALID, "%s: fluid cell index out of range (i: %d j: %d k: %d)", fn, ijk[3 * q],
+                      ijk[3 * q + 1], ijk[3 * q + 2]);
+            return GFS_ERR_INVALID;
+        }
+    }
+    return GFS_OK;
+}
+}  // namespace
+
+int gfs_sim_add_fluid_cells(gfs_sim *sim, const int32_t *ijk, int n, const float *velocity) {
+    int rc = check_cells("gfs_sim_add_fluid_cells", sim, ijk, n);
+    if (rc || n == 0) return rc;
+    Sim *s = &sim->s;
+    Ctx *ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    const int T = 256;
+    // the cells that are air now (fluidsimulation.cpp:900-902)
+    if (s->src_a.ensure((size_t)n * 3 * sizeof(int32_t)) || s->src_b.ensure((size_t)n)) return GFS_ERR_NOMEM;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(s->src_a.p, ijk, (size_t)n * 3 * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    k_cells_material<<<grid_blocks(n, T), T, 0, st>>>(s->g.c, s->mat.as<uint8_t>(), s->src_a.as<int32_t>(), n,
+                                                      s->src_b.as<uint8_t>());
+    ctx->launches++;
+    GFS_LAUNCH_CHECK();
+    std::vector<uint8_t> m((size_t)n);
+    GFS_CUDA_CHECK(cudaMemcpyAsync(m.data(), s->src_b.p, (size_t)n, cudaMemcpyDeviceToHost, st));
+    GFS_CUDA_CHECK(cudaStreamSynchronize(st));
+    Sim::CellGroup grp;
+    for (int a = 0; a < 3; a++) grp.vel[a] = velocity ? velocity[a] : 0.0f;
+    for (int q = 0; q < n; q++)
+        if (m[q] == GFS_AIR) grp.ijk.insert(grp.ijk.end(), ijk + 3 * q, ijk + 3 * q + 3);
+    if (!grp.ijk.empty()) s->added_cells.push_back(std::move(grp));
+    return GFS_OK;
+}
+
+int gfs_sim_remove_fluid_cells(gfs_sim *sim, const int32_t *ijk, int n) {
+    int rc = check_cells("gfs_sim_remove_fluid_cells", sim, ijk, n);
+    if (rc || n == 0) return rc;
+    sim->s.removed_cells.insert(sim->s.removed_cells.end(), ijk, ijk + 3 * (size_t)n);
     return GFS_OK;
 }
 

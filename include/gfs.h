@@ -272,8 +272,27 @@ int gfs_sim_set_fluid_sources(gfs_sim *sim, const gfs_fluid_source *sources, int
    the positions are the reference's exactly. */
 int gfs_sim_set_marker_particle_jitter(gfs_sim *sim, double factor, uint64_t seed);
 
-/* Apply the fluid sources once, outside a step (the source stage of
-   _updateFluidCells alone), and sort the particles.  Outputs may be NULL. */
+/* Queue n cells (int32 triples i, j, k) to become fluid at the next step, each
+   with 8 marker particles of the given velocity (float[3]; NULL: zero).
+   Replaces FluidSimulation::addFluidCells (fluidsimulation.cpp:887-918) and the
+   C exports FluidSimulation_add_fluid_cells / _add_fluid_cells_velocity
+   (c_bindings/fluidsimulation_c.cpp:770-808): only the cells that are air when
+   called are queued; an index out of range fails with GFS_ERR_INVALID and
+   queues nothing.  The next step applies the queue where the reference does
+   (_updateAddedFluidCellQueue, :1881-1892): a queued cell that is still air
+   gets its particles (the jitter of gfs_sim_set_marker_particle_jitter) and
+   becomes fluid. */
+int gfs_sim_add_fluid_cells(gfs_sim *sim, const int32_t *ijk, int n, const float *velocity);
+
+/* Queue n cells whose marker particles the next step removes, after the added
+   cells and before the fluid sources (_updateRemovedFluidCellQueue,
+   :1895-1930).  Replaces FluidSimulation::removeFluidCells (:920-940) and
+   FluidSimulation_remove_fluid_cells (c_bindings/fluidsimulation_c.cpp:810-828). */
+int gfs_sim_remove_fluid_cells(gfs_sim *sim, const int32_t *ijk, int n);
+
+/* Apply the queued fluid cells and the fluid sources once, outside a step (the
+   part of _updateFluidCells before the cells are classified, :1990-1994), and
+   sort the particles.  Outputs (totals of both) may be NULL. */
 int gfs_sim_update_fluid_sources(gfs_sim *sim, int64_t *num_added, int64_t *num_removed);
 
 /* ------------------------------------------------------------- savestates */

@@ -1,5 +1,6 @@
 """NumPy restatement of FluidSimulation::_updateFluidSources
-(fluidsimulation.cpp:1717-1879) for small grids (test infrastructure only: the
+(fluidsimulation.cpp:1717-1879) and of the fluid-cell queues
+(addFluidCells / removeFluidCells, :887-940, 1881-1930) for small grids (test infrastructure only: the
 checker for gfs_sim_update_fluid_sources and the source stage of gfs_sim_step;
 the product path never imports it).
 
@@ -103,6 +104,61 @@ def aabb(src):
     return [f32(x) for x in src["position"]], [float(x) for x in src["size"]]
 
 
+ORDER8 = [(-1, -1, -1), (1, -1, -1), (1, -1, 1), (-1, -1, 1), (-1, 1, -1), (1, 1, -1), (1, 1, 1), (-1, 1, 1)]
+
+
+def cell_particles(g, dx, nid, seed, jit):
+    """_addMarkerParticlesToCell (fluidsimulation.cpp:1223-1246): 8 positions at
+    the 2x2x2 sub-cell centres (double offsets from the float centre, stored as
+    float) plus jitter, for ids nid .. nid + 7."""
+    q = 0.25 * dx
+    cc = [cell_center(x, dx) for x in g]
+    out = []
+    for n, sgn in enumerate(ORDER8):
+        out.append(tuple(f32(f32(float(cc[a]) + sgn[a] * q) + jitter_component(seed, nid + n, a, jit))
+                         for a in range(3)))
+    return out
+
+
+def add_fluid_cells_filter(dims, mat, cells):
+    """FluidSimulation::addFluidCells (fluidsimulation.cpp:887-909): an index out
+    of range raises (nothing is queued); the cells that are air now are kept."""
+    for g in cells:
+        if not all(0 <= g[a] < dims[a] for a in range(3)):
+            raise IndexError(f"fluid cell index out of range: {tuple(g)}")
+    return [tuple(int(x) for x in g) for g in cells if mat[g[2], g[1], g[0]] == AIR]
+
+
+def update_fluid_cell_queues(dims, dx, mat, pos, vel, ids, added, removed, jitter_factor=0.1, seed=0,
+                             next_id=None):
+    """_updateAddedFluidCellQueue then _updateRemovedFluidCellQueue
+    (fluidsimulation.cpp:1881-1930) on (mat [k, j, i], pos, vel, ids).
+    added: [(cells, velocity)] groups as queued (already filtered by
+    add_fluid_cells_filter); removed: cells.  Returns (mat, pos, vel, ids, next_id)."""
+    mat = mat.copy()
+    P = [tuple(p) for p in np.asarray(pos, np.float32)]
+    V = [tuple(v) for v in np.asarray(vel, np.float32)]
+    I = [int(i) for i in ids]
+    nid = (max(I) + 1 if I else 0) if next_id is None else int(next_id)
+    jit = 0.25 * jitter_factor * dx
+    for cells, velo in added:
+        velo = tuple(f32(x) for x in velo)
+        for g in cells:                          # _addNewFluidCells (:1749-1759)
+            if mat[g[2], g[1], g[0]] != AIR:
+                continue
+            P.extend(cell_particles(g, dx, nid, seed, jit))
+            V.extend([velo] * 8)
+            I.extend(range(nid, nid + 8))
+            nid += 8
+            mat[g[2], g[1], g[0]] = FLUID
+    rm = {tuple(int(x) for x in g) for g in removed}
+    keep = np.array([pos_to_index(p, dx) not in rm for p in P], bool) if P else np.zeros(0, bool)
+    pos = np.array(P, np.float32).reshape(-1, 3)[keep]
+    vel = np.array(V, np.float32).reshape(-1, 3)[keep]
+    ids = np.array(I, np.uint32)[keep]
+    return mat, pos, vel, ids, nid
+
+
 def update_fluid_sources(dims, dx, mat, pos, vel, ids, sources, jitter_factor=0.1, seed=0, next_id=None):
     """_updateFluidSources on (mat [k, j, i], pos, vel, ids); returns the new
     (mat, pos, vel, ids): particles appended in the reference's creation order
@@ -113,8 +169,6 @@ def update_fluid_sources(dims, dx, mat, pos, vel, ids, sources, jitter_factor=0.
     I = [int(i) for i in ids]
     nid = (max(I) + 1 if I else 0) if next_id is None else int(next_id)
     jit = 0.25 * jitter_factor * dx
-    q = 0.25 * dx
-    order = [(-1, -1, -1), (1, -1, -1), (1, -1, 1), (-1, -1, 1), (-1, 1, -1), (1, 1, -1), (1, 1, 1), (-1, 1, 1)]
     for src in sources:
         if not src.get("active", True) or src.get("outflow", False):
             continue
@@ -129,13 +183,10 @@ def update_fluid_sources(dims, dx, mat, pos, vel, ids, sources, jitter_factor=0.
             if kind[g] != 1:
                 continue
             mat[g[2], g[1], g[0]] = FLUID
-            cc = [cell_center(x, dx) for x in g]
-            for sgn in order:
-                p = [f32(f32(float(cc[a]) + sgn[a] * q) + jitter_component(seed, nid, a, jit)) for a in range(3)]
-                P.append(tuple(p))
-                V.append(velo)
-                I.append(nid)
-                nid += 1
+            P.extend(cell_particles(g, dx, nid, seed, jit))
+            V.extend([velo] * 8)
+            I.extend(range(nid, nid + 8))
+            nid += 8
         # 2. empty sub-cells of fluid-or-air overlapping cells (_getNewFluidParticles)
         bp, bw = aabb(src)
         fp, fw = fit_box(bp, bw, dx, dims)

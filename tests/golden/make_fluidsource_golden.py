@@ -17,6 +17,14 @@
    defining private/protected as public in its own translation unit, after the
    standard headers; the library is compiled unchanged.
 
+4. `fluidcells_ref.state` and `fluidcells_queues.json`: the same input with
+   the same sources, plus two addFluidCells groups (one with a velocity, one
+   through the overload without; duplicates, fluid and solid cells among them)
+   and one removeFluidCells list (pool cells, a cell inside the inflow sphere,
+   an added cell), after the reference's whole _updateFluidCells (solid
+   removal, the added queue, the removed queue, the sources, classification),
+   jitter factor 0, saved with FluidSimulation::saveState.
+
 Needs the reference's source tree and g++; the fixtures are committed.
 
     python tests/golden/make_fluidsource_golden.py
@@ -46,6 +54,15 @@ SOURCES = [
     {"shape": "sphere", "position": [3.0, 0.6, 2.2], "radius": 0.45, "velocity": [0.0, 0.0, 0.0], "outflow": True},
     {"shape": "sphere", "position": [1.5, 2.5, 1.5], "radius": 0.5, "velocity": [0.0, 0.0, 0.0], "active": False},
 ]
+
+
+# addFluidCells groups (cells, velocity or None for the overload without one) and
+# the removeFluidCells list; (i, j, k) in the 16 x 14 x 12 grid above
+ADD_GROUPS = [
+    ([[3, 6, 4], [4, 6, 4], [5, 7, 5], [2, 2, 2], [3, 6, 4], [10, 9, 4]], [0.5, -0.25, 0.0]),
+    ([[4, 6, 4], [8, 9, 6], [9, 9, 6], [0, 5, 5]], None),
+]
+REMOVED = [[6, 3, 6], [7, 3, 6], [5, 7, 5], [8, 4, 6], [1, 1, 1]]
 
 
 def scene(seed=17):
@@ -78,8 +95,32 @@ def _probe_source(q, s):
     return line + add
 
 
-def probe_source():
+def _probe_cells(name, cells):
+    out = f"    std::vector<GridIndex> {name};\n"
+    for c in cells:
+        out += f"    {name}.push_back(GridIndex({c[0]}, {c[1]}, {c[2]}));\n"
+    return out
+
+
+def _probe_queues():
+    body = ""
+    for q, (cells, v) in enumerate(ADD_GROUPS):
+        body += _probe_cells(f"add{q}", cells)
+        if v is None:
+            body += f"    sim.addFluidCells(add{q});\n"
+        else:
+            body += "    sim.addFluidCells(add{}, vmath::vec3((float){!r}, (float){!r}, (float){!r}));\n".format(
+                q, *map(float, v))
+    body += _probe_cells("rem", REMOVED)
+    body += "    sim.removeFluidCells(rem);\n"
+    return body
+
+
+def probe_source(queues=False):
     body = "".join(_probe_source(q, s) for q, s in enumerate(SOURCES))
+    if queues:
+        body += _probe_queues()
+    update = "sim._updateFluidCells();" if queues else "sim._updateFluidSources();"
     return r'''
 #include <algorithm>
 #include <cmath>
@@ -106,7 +147,7 @@ int main(int argc, char **argv) {
     sim._markerParticleJitterFactor = 0.0;
 ''' + body + r'''
     int before = sim.getNumMarkerParticles();
-    sim._updateFluidSources();
+    ''' + update + r'''
     sim.saveState(argv[2]);
     std::printf("%d %d\n", before, sim.getNumMarkerParticles());
     return 0;
@@ -123,22 +164,25 @@ def main():
     S.write_state(fin, DIMS, DX, 0, pos, vel, mat)
     with open(os.path.join(HERE, "fluidsource_sources.json"), "w") as f:
         json.dump(SOURCES, f, indent=1)
+    with open(os.path.join(HERE, "fluidcells_queues.json"), "w") as f:
+        json.dump({"added": [{"cells": c, "velocity": v} for c, v in ADD_GROUPS], "removed": REMOVED}, f, indent=1)
     build.build()
     with tempfile.TemporaryDirectory() as tmp:
         out = os.path.join(tmp, "tree")
         build_reference_tree(SRC, out, opt="-O0")
-        probe = os.path.join(tmp, "probe.cpp")
-        with open(probe, "w") as f:
-            f.write(probe_source())
-        exe = os.path.join(tmp, "probe")
         lib_dir = os.path.dirname(build.LIB)
-        subprocess.run(["g++", "-std=c++11", "-O0", "-w", "-DNFLUIDSIMDEBUG", "-include", "limits", "-I" + out,
-                        "-I" + os.path.join(ROOT, "include"), probe, "-o", exe, "-L" + out, "-lfluidsim_gfs", "-Wl,-rpath," + out, "-L" + lib_dir, "-lgfs",
-                        "-Wl,-rpath," + lib_dir], check=True)
-        r = subprocess.run([exe, fin, fref], capture_output=True, text=True, timeout=300, cwd=tmp)
-        if r.returncode != 0:
-            raise RuntimeError(f"probe failed ({r.returncode}): {r.stderr[-2000:]}")
-        print("reference particles before / after:", r.stdout.strip())
+        for queues, dst in ((False, fref), (True, os.path.join(HERE, "fluidcells_ref.state"))):
+            probe = os.path.join(tmp, "probe.cpp")
+            with open(probe, "w") as f:
+                f.write(probe_source(queues))
+            exe = os.path.join(tmp, "probe")
+            subprocess.run(["g++", "-std=c++11", "-O0", "-w", "-DNFLUIDSIMDEBUG", "-include", "limits", "-I" + out,
+                            "-I" + os.path.join(ROOT, "include"), probe, "-o", exe, "-L" + out, "-lfluidsim_gfs",
+                            "-Wl,-rpath," + out, "-L" + lib_dir, "-lgfs", "-Wl,-rpath," + lib_dir], check=True)
+            r = subprocess.run([exe, fin, dst], capture_output=True, text=True, timeout=300, cwd=tmp)
+            if r.returncode != 0:
+                raise RuntimeError(f"probe failed ({r.returncode}): {r.stderr[-2000:]}")
+            print(os.path.basename(dst), "reference particles before / after:", r.stdout.strip())
 
 
 if __name__ == "__main__":

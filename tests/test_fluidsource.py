@@ -59,3 +59,38 @@ def test_jittered_particles_stay_in_their_sub_cells():
     jmax = 0.25 * 0.1 * inp["dx"]
     assert d.max() <= jmax * (1 + 1e-6) and d.max() > 0.5 * jmax
     assert np.array_equal(p1[~new], p0[~new])
+
+
+def queue_case(mat, dims):
+    """The queued groups of tests/golden/fluidcells_queues.json, filtered as
+    addFluidCells filters them when called."""
+    q = json.load(open(os.path.join(G, "fluidcells_queues.json")))
+    added = [(F.add_fluid_cells_filter(dims, mat, grp["cells"]), grp["velocity"] or [0.0, 0.0, 0.0])
+             for grp in q["added"]]
+    return added, q["removed"]
+
+
+def test_oracle_matches_reference_fluid_cell_queues():
+    """The queues, then the sources, as the reference's _updateFluidCells
+    (fluidsimulation.cpp:1990-1994) ran them."""
+    inp, _, srcs, mat = load_case()
+    ref = S.read_state(os.path.join(G, "fluidcells_ref.state"))
+    dims, dx = inp["dims"], inp["dx"]
+    added, removed = queue_case(mat, dims)
+    assert [len(c) for c, _ in added] == [5, 3]      # (2,2,2) is fluid and (0,5,5) solid: not queued
+    m, p, v, ids, nid = F.update_fluid_cell_queues(dims, dx, mat, inp["positions"], inp["velocities"],
+                                                   np.arange(len(inp["positions"])), added, removed,
+                                                   jitter_factor=0.0)
+    _, p, v, ids, _ = F.update_fluid_sources(dims, dx, m, p, v, ids, srcs, jitter_factor=0.0, next_id=nid)
+    assert len(p) == len(ref["positions"]) == 5394
+    assert np.array_equal(rows(p, v), rows(ref["positions"], ref["velocities"]))
+    assert len(np.unique(ids)) == len(ids)
+
+
+def test_fluid_cell_index_out_of_range():
+    inp, _, _, mat = load_case()
+    try:
+        F.add_fluid_cells_filter(inp["dims"], mat, [[1, 1, 1], [16, 0, 0]])
+    except IndexError:
+        return
+    raise AssertionError("out-of-range cell accepted")
