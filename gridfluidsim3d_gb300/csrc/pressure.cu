@@ -22,7 +22,11 @@
 // The CG loop runs on the device: each kernel first checks a device "done"
 // flag, reductions finish in the last CTA to arrive (fixed order, so results
 // are deterministic), and the host only polls the flag every few iterations.
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
+
+#include <cooperative_groups.h>
 
 #include "gfs_internal.h"
 
@@ -885,6 +889,295 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
     }
 }
 
+// Clustered triangular solve (FWD / BWD): k_tri with the hand-overs inside a
+// thread-block cluster moved from L2 to distributed shared memory.  A cluster
+// of CL_J x CL_K blocks takes one dispatch ticket (clusters in dependency
+// order, 4 x 2 or 2 x 2 blocks); within it, a producer block stores each edge value, tagged as in the
+// L2 exchange, straight into the consumer block's shared receive buffer, where
+// the consumer polls its own shared memory.  Hand-overs between clusters keep
+// the L2 exchange words.  On a monotone path through the 16 x 16 blocks of a
+// 256^3 grid that leaves 3 + 7 (4 x 2) or 7 + 7 (2 x 2) of the 30 hand-overs in L2.  The receive
+// buffers hold every step (no slot is reused within a launch), so producers
+// need no flow control; a cluster barrier after zeroing them orders the first
+// remote store after the zeroing, and one before exit keeps every block
+// resident while its peers may still store into it.  Arithmetic, summation
+// order and outputs are k_tri's.
+template <class T>
+__device__ __forceinline__ T rx_take(const unsigned long long *p, unsigned tag, PsCtrl *ctrl, bool &timed_out) {
+    using X = Xch<T>;
+    unsigned long long w[X::W];
+#pragma unroll
+    for (int q = 0; q < X::W; q++) w[q] = *(const volatile unsigned long long *)(p + q);
+    if (!X::ready(w, tag) && !timed_out) {
+        int spins = 0;
+        do {
+#pragma unroll
+            for (int q = 0; q < X::W; q++) w[q] = *(const volatile unsigned long long *)(p + q);
+            if (++spins > GFS_SPIN_LIMIT) {
+                atomicOr(&ctrl->err, GFS_DEV_ERR_TIMEOUT);
+                timed_out = true;
+                break;
+            }
+        } while (!X::ready(w, tag));
+    }
+    return X::value(w);
+}
+
+template <class T>
+__device__ __forceinline__ void rx_put(unsigned long long *p, T v, unsigned tag) {
+    if constexpr (sizeof(T) == 4) {
+        *(volatile unsigned long long *)p = ((unsigned long long)tag << 32) | (unsigned long long)__float_as_uint(v);
+    } else {
+        unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+        *(volatile unsigned long long *)p = ((unsigned long long)tag << 32) | (bits & 0xFFFFFFFFull);
+        *(volatile unsigned long long *)(p + 1) = ((unsigned long long)tag << 32) | (bits >> 32);
+    }
+}
+
+// receive-buffer steps: the first edge value a producer hands over is its step SBJ-1 (= SBK-1)
+__host__ __device__ __forceinline__ int rx_steps(int S) { return S - (SBJ - 1); }
+
+template <class T, int MODE, int P, int PE, int CL_J, int CL_K>
+__global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE, 1) k_tri_cl(SweepArgs<T> A) {
+    namespace cg = cooperative_groups;
+    using Op = Ar<T>;
+    using X = Xch<T>;
+    static_assert(MODE == SW_FWD || MODE == SW_BWD, "triangular solves only");
+    static_assert(SBJ == SBK, "one receive-buffer step count for both edges");
+    constexpr bool bwd = MODE == SW_BWD;
+    constexpr long long PS = bwd ? -(long long)SPLANE : (long long)SPLANE;
+    constexpr long long XP = (long long)XCH_PER_PLANE * X::W;
+    constexpr long long XS = bwd ? -XP : XP;
+    constexpr int NARR = bwd ? 3 : 2;
+    constexpr int W = X::W;
+    __shared__ T xb[2][SBK][SBJ];
+    __shared__ __align__(16) T ring[NARR][P][SPLANE];
+    __shared__ unsigned sh_ticket, sh_epoch;
+    // receive buffers: j edge [step][kl][W], then k edge [step][jl][W]
+    extern __shared__ __align__(16) unsigned long long rx[];
+    if (A.ctrl->done) return;   // the same value in every block of the launch
+    cg::cluster_group cl = cg::this_cluster();
+    const unsigned rank = cl.block_rank();
+    const int tid = threadIdx.x;
+    const Skew &K = A.K;
+    const int S = K.S;
+    const int NR = rx_steps(S);
+    unsigned long long *rxj = rx, *rxk = rx + (long long)NR * SBK * W;
+    for (int q = tid; q < 2 * NR * SBK * W; q += SPLANE) rx[q] = 0ull;
+    if (tid == 0) {
+        if (rank == 0) sh_ticket = atomicAdd(A.ticket, 1u);
+        sh_epoch = A.ctrl->epoch;
+    }
+    cl.sync();
+    const unsigned t = *cl.map_shared_rank(&sh_ticket, 0u), tag = sh_epoch;
+    const int ncj = (K.nbj + CL_J - 1) / CL_J, nck = (K.nbk + CL_K - 1) / CL_K;
+    int cj = (int)(t % (unsigned)ncj), ck = (int)(t / (unsigned)ncj);
+    if (bwd) {
+        cj = ncj - 1 - cj;
+        ck = nck - 1 - ck;
+    }
+    const int j0 = cj * CL_J, k0 = ck * CL_K;
+    const int bj = j0 + (int)(rank % CL_J), bk = k0 + (int)(rank / CL_J);
+    const bool exists = bj < K.nbj && bk < K.nbk;
+    const bool live = exists && A.blkf[bk * K.nbj + bj] != 0;
+    const int pbj = bwd ? bj + 1 : bj - 1, pbk = bwd ? bk + 1 : bk - 1;
+    const int cbj = bwd ? bj - 1 : bj + 1, cbk = bwd ? bk - 1 : bk + 1;
+    const bool has_pj = exists && pbj >= 0 && pbj < K.nbj && A.blkf[bk * K.nbj + pbj],
+               has_pk = exists && pbk >= 0 && pbk < K.nbk && A.blkf[pbk * K.nbj + bj];
+    const bool has_cj = exists && cbj >= 0 && cbj < K.nbj && A.blkf[bk * K.nbj + cbj],
+               has_ck = exists && cbk >= 0 && cbk < K.nbk && A.blkf[cbk * K.nbj + bj];
+    // neighbours inside this cluster hand over through shared memory
+    const bool pj_cl = pbj >= j0 && pbj < j0 + CL_J, pk_cl = pbk >= k0 && pbk < k0 + CL_K;
+    const bool cj_cl = cbj >= j0 && cbj < j0 + CL_J, ck_cl = cbk >= k0 && cbk < k0 + CL_K;
+    bool timed_out = false;
+
+    const int jl = tid % SBJ, kl = tid / SBJ;
+    const bool valid = live && bj * SBJ + jl < K.ny && bk * SBK + kl < K.nz;
+    const int xj = bwd ? jl + 1 : jl - 1, xk = bwd ? kl + 1 : kl - 1;
+    const bool at_j = bwd ? jl == SBJ - 1 : jl == 0;
+    const bool at_k = bwd ? kl == SBK - 1 : kl == 0;
+    const bool in_j = at_j && has_pj, in_k = at_k && has_pk;
+    const bool in_jx = in_j && !pj_cl, in_kx = in_k && !pk_cl;   // through L2
+    const bool out_j = (bwd ? jl == 0 : jl == SBJ - 1) && has_cj;
+    const bool out_k = (bwd ? kl == 0 : kl == SBK - 1) && has_ck;
+    const bool out_jx = out_j && !cj_cl, out_kx = out_k && !ck_cl;
+    const int st_lo = valid ? (bwd ? S - K.nx - jl - kl : jl + kl) : S;
+    const int st_hi = valid ? st_lo + K.nx : S;
+    const long long q0 = K.base(bj, bk) + kl * SBJ + jl + (bwd ? (long long)(S - 1) * SPLANE : 0);
+    // inputs: each plane of a block is SPLANE contiguous slots, copied in 16-byte
+    // pieces by the first NCP threads (16-byte aligned: allocation bases, and
+    // plane offsets that are multiples of SPLANE elements)
+    constexpr int E = 16 / (int)sizeof(T), NCP = SPLANE / E;
+    const bool copier = tid < NCP;
+    const long long qp = K.base(bj, bk) + (bwd ? (long long)(S - 1) * SPLANE : 0) + (long long)tid * E;
+    const T *ca = A.in + qp, *cb = A.precon + qp, *cc = (bwd ? A.rdot : A.in) + qp;
+    const T *fa = ca + P * PS, *fb = cb + P * PS, *fc = cc + P * PS;
+    T *po = A.out + q0;
+    const long long xblock = (long long)S * XP;
+    unsigned long long *xbuf = A.xch;
+    const long long bself = exists ? (long long)(bk * K.nbj + bj) * xblock : 0;
+    unsigned long long *pxj_out = xbuf + bself + (bwd ? (long long)(S - 1) * XP : 0) + (long long)kl * W;
+    unsigned long long *pxk_out = xbuf + bself + (bwd ? (long long)(S - 1) * XP : 0) + (long long)(SBJ + jl) * W;
+    const unsigned long long *pxj_in =
+        xbuf + (has_pj ? (long long)(bk * K.nbj + pbj) * xblock +
+                             (bwd ? (long long)(S - 1 - (SBJ - 1)) : (long long)(SBJ - 1)) * XP + (long long)kl * W
+                       : 0);
+    const unsigned long long *pxk_in =
+        xbuf + (has_pk ? (long long)(pbk * K.nbj + bj) * xblock +
+                             (bwd ? (long long)(S - 1 - (SBK - 1)) : (long long)(SBK - 1)) * XP +
+                             (long long)(SBJ + jl) * W
+                       : 0);
+    // this thread's receive words (step 0) and, on a downstream edge inside the
+    // cluster, the consumer's (its step 0 is this block's step SBJ-1)
+    const unsigned long long *rj_in = rxj + (long long)kl * W;
+    const unsigned long long *rk_in = rxk + (long long)jl * W;
+    unsigned long long *rj_out = nullptr, *rk_out = nullptr;
+    if (out_j && cj_cl) rj_out = cl.map_shared_rank(rxj, rank + (unsigned)(cbj - bj)) + (long long)kl * W;
+    if (out_k && ck_cl) rk_out = cl.map_shared_rank(rxk, rank + (unsigned)((cbk - bk) * CL_J)) + (long long)jl * W;
+
+#pragma unroll
+    for (int u = 0; u < P; u++) {
+        if (copier && u < S && live) {
+            cp_async<16>(&ring[0][u][tid * E], ca + u * PS, true);
+            cp_async<16>(&ring[1][u][tid * E], cb + u * PS, true);
+            if (bwd) cp_async<16>(&ring[NARR - 1][u][tid * E], cc + u * PS, true);
+        }
+        cp_async_commit();
+    }
+    cp_async_wait<P - 1>();   // step 0 has landed ...
+    __syncthreads();          // ... and is visible to every thread
+    unsigned long long r_wj[PE][W], r_wk[PE][W];
+#pragma unroll
+    for (int v = 0; v < PE; v++) {
+        const bool ok = v >= st_lo && v < st_hi;
+        if (in_jx && ok) X::fetch(pxj_in + v * XS, r_wj[v]);
+        if (in_kx && ok) X::fetch(pxk_in + v * XS, r_wk[v]);
+    }
+
+    T prev = T(0);
+    Acc2f dot32;
+    double dot64 = 0.0;
+    static_assert(P % PE == 0, "exchange ring must divide the input ring");
+    const int SP = live ? ((S + P - 1) / P) * P : 0;
+    for (int s0 = 0; s0 < SP; s0 += P) {
+#pragma unroll
+        for (int u = 0; u < P; u++) {
+            const int st = s0 + u;
+            const int v = u % PE;
+            // the slot step st-1 read is free (the barrier of step st-1 has passed):
+            // refill it with step st-1+P
+            if (st >= 1) {
+                if (copier && st - 1 + P < S) {
+                    cp_async<16>(&ring[0][(u + P - 1) % P][tid * E], fa, true);
+                    cp_async<16>(&ring[1][(u + P - 1) % P][tid * E], fb, true);
+                    if (bwd) cp_async<16>(&ring[NARR - 1][(u + P - 1) % P][tid * E], fc, true);
+                }
+                fa += PS;
+                fb += PS;
+                fc += PS;
+            }
+            cp_async_commit();
+            const bool act = st >= st_lo && st < st_hi;
+            T nj_ = at_j ? T(0) : xb[(st - 1) & 1][kl][xj];
+            T nk_ = at_k ? T(0) : xb[(st - 1) & 1][xk][jl];
+            if (in_j && act)
+                nj_ = pj_cl ? rx_take<T>(rj_in + (long long)st * SBK * W, tag, A.ctrl, timed_out)
+                            : xch_take<T>(r_wj[v], pxj_in + (long long)st * XS, tag, A.ctrl, timed_out);
+            if (in_k && act)
+                nk_ = pk_cl ? rx_take<T>(rk_in + (long long)st * SBJ * W, tag, A.ctrl, timed_out)
+                            : xch_take<T>(r_wk[v], pxk_in + (long long)st * XS, tag, A.ctrl, timed_out);
+            const T ra = ring[0][u][tid], pc = ring[1][u][tid];
+            T val, xch;
+            if (MODE == SW_FWD) {
+                // _applyPreconditioner forward solve (pressuresolver.cpp:311-351)
+                val = Op::mul(Op::sub(Op::sub(Op::sub(ra, prev), nj_), nk_), pc);
+                xch = Op::mul(Op::mul(A.negscale, pc), val);
+            } else {
+                // backward solve (pressuresolver.cpp:354-385)
+                const T m = Op::mul(A.negscale, pc);
+                val = Op::mul(Op::sub(Op::sub(Op::sub(ra, Op::mul(m, prev)), Op::mul(m, nj_)), Op::mul(m, nk_)), pc);
+                xch = val;
+            }
+            val = act ? val : T(0);
+            xch = act ? xch : T(0);
+            if (MODE == SW_BWD && act) {
+                const T rv = ring[NARR - 1][u][tid];
+                if (sizeof(T) == 4) dot32.add((float)val * (float)rv);
+                else dot64 += (double)val * (double)rv;
+            }
+            if (st < S) {
+                *po = val;
+                if (out_j && act) {
+                    if (rj_out) rx_put<T>(rj_out + (long long)(st - (SBJ - 1)) * SBK * W, xch, tag);
+                    else X::put(pxj_out, xch, tag);
+                }
+                if (out_k && act) {
+                    if (rk_out) rx_put<T>(rk_out + (long long)(st - (SBK - 1)) * SBJ * W, xch, tag);
+                    else X::put(pxk_out, xch, tag);
+                }
+            }
+            po += PS;
+            pxj_out += XS;
+            pxk_out += XS;
+            xb[st & 1][kl][jl] = xch;
+            prev = xch;
+            {
+                const int sx = st + PE;
+                const bool ok = sx >= st_lo && sx < st_hi;
+                if (in_jx && ok) X::fetch(pxj_in + (long long)sx * XS, r_wj[v]);
+                if (in_kx && ok) X::fetch(pxk_in + (long long)sx * XS, r_wk[v]);
+            }
+            cp_async_wait<P - 2>();   // step st+1 has landed (its group is older than the last P-2)
+            __syncthreads();
+        }
+    }
+    cp_async_wait<0>();
+    // no block of the cluster leaves while a peer may still store into it
+    cl.sync();
+
+    double part = 0.0;
+    if (MODE == SW_BWD) part = block_reduce<0>(sizeof(T) == 4 ? dot32.value() : dot64);
+    __shared__ bool last;
+    if (tid == 0) {
+        if (MODE == SW_BWD && exists) A.partials[bj + K.nbj * bk] = part;
+        __threadfence();
+        unsigned tk = atomicAdd(A.done_ticket, 1u);
+        last = tk == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (MODE == SW_BWD) {
+        const unsigned nblocks = (unsigned)(K.nbj * K.nbk);
+        double acc = 0.0;
+        for (unsigned q = tid; q < nblocks; q += SPLANE) acc += __ldcg(A.partials + q);
+        acc = block_reduce<0>(acc);
+        if (tid == 0) {
+            PsCtrl *C = A.ctrl;
+            if (A.init) {
+                C->sigma = acc;
+                C->beta = 0.0;
+            } else {
+                // _solvePressureSystem (pressuresolver.cpp:481-486)
+                C->beta = acc / C->sigma;
+                C->sigma = acc;
+                C->iter += 1;
+                if (C->iter >= C->max_iters) C->done = 1;
+            }
+        }
+    }
+    if (tid == 0) {
+        *A.ticket = 0;
+        *A.done_ticket = 0;
+        A.ctrl->epoch = tag + 1 == 0 ? 1u : tag + 1;
+    }
+}
+
+// dynamic shared memory of k_tri_cl: the two receive buffers
+template <class T>
+static size_t tri_cl_smem(int S) {
+    return (size_t)2 * rx_steps(S) * SBJ * Xch<T>::W * sizeof(unsigned long long);
+}
 // -------------------------------------------------------- vector kernels
 
 template <class T>
@@ -1304,6 +1597,60 @@ static int ensure_ws(Ctx *ctx, PressureWs &ws, const Grids &g, bool mixed) {
     return GFS_OK;
 }
 
+// The clustered triangular solves run unless GFS_SWEEP_CLUSTER=0 is set in the
+// environment when the library first solves (then k_tri runs everywhere).
+static bool sweep_cluster_enabled() {
+    static const bool on = [] {
+        const char *e = getenv("GFS_SWEEP_CLUSTER");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+// k_tri_cl<.., CJ, CK> fits when its receive buffers fit in shared memory and
+// every cluster of the launch can be resident at once (a cluster that waits for
+// a free SM would serialise the wavefront); checked, and the shared-memory
+// limit raised, once per instantiation and size.
+template <class T, int MODE, int P, int PE, int CJ, int CK>
+static bool tri_cl_usable(int S, int ncl) {
+    static std::mutex mu;
+    static size_t attr = 0;
+    static int active = -1;   // clusters that fit at once, -1 unknown
+    const size_t dyn = tri_cl_smem<T>(S);
+    if (dyn > 160 * 1024) return false;
+    std::lock_guard<std::mutex> lock(mu);
+    if (dyn > attr) {
+        if (cudaFuncSetAttribute(k_tri_cl<T, MODE, P, PE, CJ, CK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)dyn) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        attr = dyn;
+        active = -1;
+    }
+    if (active < 0) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(CJ * CK);
+        cfg.blockDim = dim3(SPLANE);
+        cfg.dynamicSmemBytes = attr;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, k_tri_cl<T, MODE, P, PE, CJ, CK>, &cfg) != cudaSuccess) n = 0;
+        cudaGetLastError();
+        active = n;
+    }
+    return active >= ncl;
+}
+
+template <class T, int MODE, int P, int PE, int CJ, int CK>
+static bool launch_tri_cl(Ctx *ctx, const SweepArgs<T> &A) {
+    const int ncl = ((A.K.nbj + CJ - 1) / CJ) * ((A.K.nbk + CK - 1) / CK);
+    auto a16 = [](const void *q) { return ((uintptr_t)q & 15u) == 0; };
+    if (!a16(A.in) || !a16(A.precon) || (MODE == SW_BWD && !a16(A.rdot))) return false;   // 16-byte copies
+    if (!tri_cl_usable<T, MODE, P, PE, CJ, CK>(A.K.S, ncl)) return false;
+    k_tri_cl<T, MODE, P, PE, CJ, CK><<<ncl * CJ * CK, SPLANE, tri_cl_smem<T>(A.K.S), ctx->stream>>>(A);
+    return true;
+}
+
 // PE: how many steps ahead a pencil on a block edge loads the upstream block's
 // exchange words (the L2 round trip must fit in PE steps)
 #ifndef GFS_SWEEP_PE
@@ -1339,7 +1686,8 @@ static int launch_sweep(Ctx *ctx, PressureWs &ws, const T *in, T *out, const T *
     // the build runs k_sweep, the triangular solves k_tri (only the launched kernel is instantiated)
     if constexpr (MODE == SW_PRECON)
         k_sweep<T, MODE, P, PE><<<A.K.nbj * A.K.nbk, SWEEP_THREADS, 0, ctx->stream>>>(A);
-    else
+    else if (!(sweep_cluster_enabled() && (launch_tri_cl<T, MODE, P, PE, 4, 2>(ctx, A) ||
+                                           launch_tri_cl<T, MODE, P, PE, 2, 2>(ctx, A))))
         k_tri<T, MODE, P, PE><<<A.K.nbj * A.K.nbk, SPLANE, 0, ctx->stream>>>(A);
     ctx->launches++;
     GFS_LAUNCH_CHECK();
