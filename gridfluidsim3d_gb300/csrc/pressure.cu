@@ -1005,11 +1005,13 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE, 1)
     const int st_hi = valid ? st_lo + K.nx : S;
     const long long q0 = K.base(bj, bk) + kl * SBJ + jl + (bwd ? (long long)(S - 1) * SPLANE : 0);
     // inputs: each plane of a block is SPLANE contiguous slots, copied in 16-byte
-    // pieces by the first NCP threads (16-byte aligned: allocation bases, and
-    // plane offsets that are multiples of SPLANE elements)
+    // pieces by NCP threads starting at thread NCP, so that the first and last
+    // warps, which carry the k-edge exchange, copy nothing in FP32 (16-byte
+    // aligned: allocation bases, and plane offsets that are multiples of SPLANE)
     constexpr int E = 16 / (int)sizeof(T), NCP = SPLANE / E;
-    const bool copier = tid < NCP;
-    const long long qp = K.base(bj, bk) + (bwd ? (long long)(S - 1) * SPLANE : 0) + (long long)tid * E;
+    const int cpi = tid - NCP;
+    const bool copier = cpi >= 0 && cpi < NCP;
+    const long long qp = K.base(bj, bk) + (bwd ? (long long)(S - 1) * SPLANE : 0) + (long long)(copier ? cpi : 0) * E;
     const T *ca = A.in + qp, *cb = A.precon + qp, *cc = (bwd ? A.rdot : A.in) + qp;
     const T *fa = ca + P * PS, *fb = cb + P * PS, *fc = cc + P * PS;
     T *po = A.out + q0;
@@ -1038,9 +1040,9 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE, 1)
 #pragma unroll
     for (int u = 0; u < P; u++) {
         if (copier && u < S && live) {
-            cp_async<16>(&ring[0][u][tid * E], ca + u * PS, true);
-            cp_async<16>(&ring[1][u][tid * E], cb + u * PS, true);
-            if (bwd) cp_async<16>(&ring[NARR - 1][u][tid * E], cc + u * PS, true);
+            cp_async<16>(&ring[0][u][cpi * E], ca + u * PS, true);
+            cp_async<16>(&ring[1][u][cpi * E], cb + u * PS, true);
+            if (bwd) cp_async<16>(&ring[NARR - 1][u][cpi * E], cc + u * PS, true);
         }
         cp_async_commit();
     }
@@ -1066,11 +1068,11 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE, 1)
             const int v = u % PE;
             // the slot step st-1 read is free (the barrier of step st-1 has passed):
             // refill it with step st-1+P
-            if (st >= 1) {
-                if (copier && st - 1 + P < S) {
-                    cp_async<16>(&ring[0][(u + P - 1) % P][tid * E], fa, true);
-                    cp_async<16>(&ring[1][(u + P - 1) % P][tid * E], fb, true);
-                    if (bwd) cp_async<16>(&ring[NARR - 1][(u + P - 1) % P][tid * E], fc, true);
+            if (copier && st >= 1) {   // warp-uniform: the other warps skip it
+                if (st - 1 + P < S) {
+                    cp_async<16>(&ring[0][(u + P - 1) % P][cpi * E], fa, true);
+                    cp_async<16>(&ring[1][(u + P - 1) % P][cpi * E], fb, true);
+                    if (bwd) cp_async<16>(&ring[NARR - 1][(u + P - 1) % P][cpi * E], fc, true);
                 }
                 fa += PS;
                 fb += PS;
@@ -1109,16 +1111,14 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE, 1)
                 *po = val;
                 if (out_j && act) {
                     if (rj_out) rx_put<T>(rj_out + (long long)(st - (SBJ - 1)) * SBK * W, xch, tag);
-                    else X::put(pxj_out, xch, tag);
+                    else X::put(pxj_out + (long long)st * XS, xch, tag);
                 }
                 if (out_k && act) {
                     if (rk_out) rx_put<T>(rk_out + (long long)(st - (SBK - 1)) * SBJ * W, xch, tag);
-                    else X::put(pxk_out, xch, tag);
+                    else X::put(pxk_out + (long long)st * XS, xch, tag);
                 }
             }
             po += PS;
-            pxj_out += XS;
-            pxk_out += XS;
             xb[st & 1][kl][jl] = xch;
             prev = xch;
             {
