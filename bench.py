@@ -70,10 +70,11 @@ BYTES = {
 }
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# FP32 sweeps on this exact workload, from one ncu --set full capture of the
-# 5th/6th k_tri launches of this bench's mixed run.  The sweeps stream the whole dense
-# skewed grid, so the figure depends on the grid, not on the fluid-cell count.
-TRAFFIC = {"mic0_forward": 209.6e6, "mic0_backward": 292.7e6}
+# FP32 sweeps (the clustered k_tri_cl) on this exact workload, from one ncu capture
+# of the 5th/6th k_tri_cl launches of this bench's mixed run.  A sweep streams every
+# plane of each block that holds fluid (134 of the 256 blocks here), air and
+# padding slots included.
+TRAFFIC = {"mic0_forward": 91.3e6, "mic0_backward": 135.0e6}
 
 
 def rank_info():

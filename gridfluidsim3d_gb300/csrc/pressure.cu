@@ -18,6 +18,8 @@
 // later and only re-reads it (bounded) if the tag is not yet this sweep's, so
 // no fence or progress counter sits on the per-step path.  CTAs take dispatch
 // tickets in dependency order, so every CTA they wait for is already resident.
+// The FP32 triangular solves normally run k_tri_cl, the same wavefront in
+// thread-block clusters whose blocks hand over through distributed shared memory.
 //
 // The CG loop runs on the device: each kernel first checks a device "done"
 // flag, reductions finish in the last CTA to arrive (fixed order, so results
