@@ -746,10 +746,16 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
     const int st_lo = valid ? (bwd ? S - K.nx - jl - kl : jl + kl) : S;
     const int st_hi = valid ? st_lo + K.nx : S;
     const long long q0 = K.base(bj, bk) + kl * SBJ + jl + (bwd ? (long long)(S - 1) * SPLANE : 0);
-    // input pointers at step P (the first refill), output pointer at step 0
-    const T *fa = A.in + q0 + P * PS;
-    const T *fb = A.precon + q0 + P * PS;
-    const T *fc = (bwd ? A.rdot : A.in) + q0 + P * PS;
+    // inputs: each plane of a block is SPLANE contiguous slots, copied in 16-byte
+    // pieces by NCP threads starting at thread NCP (the first and last warps
+    // carry the k-edge exchange); 16-byte aligned: allocation bases, and plane
+    // offsets that are multiples of SPLANE elements
+    constexpr int E = 16 / (int)sizeof(T), NCP = SPLANE / E;
+    const int cpi = tid - NCP;
+    const bool copier = cpi >= 0 && cpi < NCP;
+    const long long qp = K.base(bj, bk) + (bwd ? (long long)(S - 1) * SPLANE : 0) + (long long)(copier ? cpi : 0) * E;
+    const T *ca = A.in + qp, *cb = A.precon + qp, *cc = (bwd ? A.rdot : A.in) + qp;
+    const T *fa = ca + P * PS, *fb = cb + P * PS, *fc = cc + P * PS;   // the first refill: step P
     T *po = A.out + q0;
     const long long xblock = (long long)S * XP;
     unsigned long long *xbuf = A.xch;
@@ -770,13 +776,15 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
     // fill the ring with steps 0..P-1
 #pragma unroll
     for (int u = 0; u < P; u++) {
-        if (u < S && live) {
-            cp_async<sizeof(T)>(&ring[0][u][tid], A.in + q0 + u * PS, true);
-            cp_async<sizeof(T)>(&ring[1][u][tid], A.precon + q0 + u * PS, true);
-            if (bwd) cp_async<sizeof(T)>(&ring[NARR - 1][u][tid], A.rdot + q0 + u * PS, true);
+        if (copier && u < S && live) {
+            cp_async<16>(&ring[0][u][cpi * E], ca + u * PS, true);
+            cp_async<16>(&ring[1][u][cpi * E], cb + u * PS, true);
+            if (bwd) cp_async<16>(&ring[NARR - 1][u][cpi * E], cc + u * PS, true);
         }
         cp_async_commit();
     }
+    cp_async_wait<P - 1>();   // step 0 has landed ...
+    __syncthreads();          // ... and is visible to every thread
     unsigned long long r_wj[PE][X::W], r_wk[PE][X::W];
 #pragma unroll
     for (int v = 0; v < PE; v++) {
@@ -795,7 +803,19 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
         for (int u = 0; u < P; u++) {
             const int st = s0 + u;
             const int v = u % PE;
-            cp_async_wait<P - 1>();
+            // the slot step st-1 read is free (the barrier of step st-1 has passed):
+            // refill it with step st-1+P
+            if (copier && st >= 1) {   // warp-uniform: the other warps skip it
+                if (st - 1 + P < S) {
+                    cp_async<16>(&ring[0][(u + P - 1) % P][cpi * E], fa, true);
+                    cp_async<16>(&ring[1][(u + P - 1) % P][cpi * E], fb, true);
+                    if (bwd) cp_async<16>(&ring[NARR - 1][(u + P - 1) % P][cpi * E], fc, true);
+                }
+                fa += PS;
+                fb += PS;
+                fc += PS;
+            }
+            cp_async_commit();
             const bool act = st >= st_lo && st < st_hi;
             T nj_ = at_j ? T(0) : xb[(st - 1) & 1][kl][xj];
             T nk_ = at_k ? T(0) : xb[(st - 1) & 1][xk][jl];
@@ -824,30 +844,19 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
             }
             if (st < S) {
                 *po = val;
-                if (out_j && act) X::put(pxj_out, xch, tag);
-                if (out_k && act) X::put(pxk_out, xch, tag);
+                if (out_j && act) X::put(pxj_out + (long long)st * XS, xch, tag);
+                if (out_k && act) X::put(pxk_out + (long long)st * XS, xch, tag);
             }
             po += PS;
-            pxj_out += XS;
-            pxk_out += XS;
             xb[st & 1][kl][jl] = xch;
             prev = xch;
-            // refill this slot with step st + P
-            if (st + P < S) {
-                cp_async<sizeof(T)>(&ring[0][u][tid], fa, true);
-                cp_async<sizeof(T)>(&ring[1][u][tid], fb, true);
-                if (bwd) cp_async<sizeof(T)>(&ring[NARR - 1][u][tid], fc, true);
-            }
-            cp_async_commit();
-            fa += PS;
-            fb += PS;
-            fc += PS;
             {
                 const int sx = st + PE;
                 const bool ok = sx >= st_lo && sx < st_hi;
                 if (in_j && ok) Xch<T>::fetch(pxj_in + (long long)sx * XS, r_wj[v]);
                 if (in_k && ok) Xch<T>::fetch(pxk_in + (long long)sx * XS, r_wk[v]);
             }
+            cp_async_wait<P - 2>();   // step st+1 has landed (its group is older than the last P-2)
             __syncthreads();
         }
     }
@@ -1662,6 +1671,14 @@ template <class T, int MODE, int P = (sizeof(T) == 8 ? 4 : 8),
           int PE = (GFS_SWEEP_PE < P ? GFS_SWEEP_PE : P)>
 static int launch_sweep(Ctx *ctx, PressureWs &ws, const T *in, T *out, const T *precon, const T *rdot,
                         float *out32, double scale, int init) {
+    if (MODE != SW_PRECON) {
+        // the triangular solves copy their input planes in 16-byte pieces
+        auto a16 = [](const void *q) { return ((uintptr_t)q & 15u) == 0; };
+        if (!a16(in) || !a16(precon) || (MODE == SW_BWD && !a16(rdot))) {
+            set_error(GFS_ERR_INVALID, "pressure sweep: input vectors must be 16-byte aligned");
+            return GFS_ERR_INVALID;
+        }
+    }
     SweepArgs<T> A;
     A.K = make_skew(ws.c);
     A.c = ws.c;
