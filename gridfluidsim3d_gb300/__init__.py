@@ -7,6 +7,7 @@ package is its host-side mirror; importing it needs no GPU, calling into it
 does, and there is no CPU fallback.
 """
 from ._lib import GFSError, PRECISION_MIXED, PRECISION_PLAIN  # noqa: F401
+from . import config  # noqa: F401
 from .core import (AIR, FLUID, SOLID, CLScalarField, Context, CuboidFluidSource, FluidSimulation,  # noqa: F401
                    FluidSimulationSaveState, FluidSource, MACVelocityField, SphericalFluidSource, ParticleAdvector, PressureSolver,
                    PressureSolverParameters, face_shape)
@@ -14,4 +15,4 @@ from .core import (AIR, FLUID, SOLID, CLScalarField, Context, CuboidFluidSource,
 __all__ = ["GFSError", "PRECISION_PLAIN", "PRECISION_MIXED", "AIR", "FLUID", "SOLID", "Context",
            "CLScalarField", "ParticleAdvector", "PressureSolver", "PressureSolverParameters",
            "MACVelocityField", "FluidSimulation", "FluidSimulationSaveState", "FluidSource", "SphericalFluidSource", "CuboidFluidSource",
-           "face_shape"]
+           "face_shape", "config"]

@@ -26,7 +26,7 @@ import os
 
 import numpy as np
 
-from . import _lib
+from . import _lib, config
 from ._lib import GFSError, PRECISION_MIXED, PRECISION_PLAIN, SimParams, StepStats
 
 AIR, FLUID, SOLID = 0, 1, 2
@@ -332,6 +332,7 @@ class FluidSimulation:
         _lib.lib().gfs_sim_default_params(ctypes.byref(self._params))
         self.last_stats = None
         self.current_frame = 0
+        self._autosave = False
 
     # -- parameters (fluidsimulation.h:146-446 setters) --
     def _push(self):
@@ -524,11 +525,30 @@ class FluidSimulation:
         sim.load_state(st.filename)
         return sim
 
+    # -- autosave (fluidsimulation.cpp:566-582, 3412-3415; pyfluid/fluidsimulation.py:496-509) --
+    @property
+    def enable_autosave(self) -> bool:
+        """When set, update() first writes the state to
+        `config.get_savestates_directory()/autosave.state`, as the reference's
+        update does at the start of every frame.  Off by default: the reference
+        enables it by default, but at 40M particles every save writes 1.1 GB."""
+        return self._autosave
+
+    @enable_autosave.setter
+    def enable_autosave(self, value):
+        self._autosave = bool(value)
+
+    def autosave_path(self) -> str:
+        return os.path.join(config.get_savestates_directory(), "autosave.state")
+
     # -- stepping --
     def update(self, dt) -> dict:
         """One substep of length dt (FluidSimulation::update, fluidsimulation.cpp:3417-3455)."""
         if dt < 0.0:
             raise GFSError(_lib.GFS_ERR_INVALID, "update", f"delta time must be >= 0 (got {dt})")
+        if self._autosave:                 # _autosave, before the frame's substeps (:3433-3435)
+            os.makedirs(config.get_savestates_directory(), exist_ok=True)
+            self.save_state(self.autosave_path())
         if getattr(self, "_sources", None):
             self._push_sources()          # sources are mutable objects, as in pyfluid
         st = StepStats()
