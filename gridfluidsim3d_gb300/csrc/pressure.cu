@@ -1621,15 +1621,23 @@ static bool sweep_cluster_enabled() {
 // k_tri_cl<.., CJ, CK> fits when its receive buffers fit in shared memory and
 // every cluster of the launch can be resident at once (a cluster that waits for
 // a free SM would serialise the wavefront); checked, and the shared-memory
-// limit raised, once per instantiation and size.
+// limit raised, once per instantiation, device and size.
 template <class T, int MODE, int P, int PE, int CJ, int CK>
 static bool tri_cl_usable(int S, int ncl) {
+    constexpr int MAXDEV = 64;
     static std::mutex mu;
-    static size_t attr = 0;
-    static int active = -1;   // clusters that fit at once, -1 unknown
+    static size_t attr_dev[MAXDEV] = {};
+    static int active_dev[MAXDEV] = {};   // clusters that fit at once, 0 unknown (stored + 1)
     const size_t dyn = tri_cl_smem<T>(S);
     if (dyn > 160 * 1024) return false;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAXDEV) {
+        cudaGetLastError();
+        return false;
+    }
     std::lock_guard<std::mutex> lock(mu);
+    size_t &attr = attr_dev[dev];
+    int &active1 = active_dev[dev];
     if (dyn > attr) {
         if (cudaFuncSetAttribute(k_tri_cl<T, MODE, P, PE, CJ, CK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)dyn) != cudaSuccess) {
@@ -1637,9 +1645,9 @@ static bool tri_cl_usable(int S, int ncl) {
             return false;
         }
         attr = dyn;
-        active = -1;
+        active1 = 0;
     }
-    if (active < 0) {
+    if (active1 == 0) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(CJ * CK);
         cfg.blockDim = dim3(SPLANE);
@@ -1647,9 +1655,9 @@ static bool tri_cl_usable(int S, int ncl) {
         int n = 0;
         if (cudaOccupancyMaxActiveClusters(&n, k_tri_cl<T, MODE, P, PE, CJ, CK>, &cfg) != cudaSuccess) n = 0;
         cudaGetLastError();
-        active = n;
+        active1 = n + 1;
     }
-    return active >= ncl;
+    return active1 - 1 >= ncl;
 }
 
 template <class T, int MODE, int P, int PE, int CJ, int CK>
