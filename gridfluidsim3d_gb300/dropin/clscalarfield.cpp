@@ -19,7 +19,7 @@ void CLScalarField::_splat(const char *where, std::vector<vmath::vec3> &points, 
                            double radius, vmath::vec3 offset, double dx, Array3d<float> *field,
                            Array3d<float> *weightfield) {
     if (!_isOpenCLEnabled) {
-        std::cerr << where << ": the accelerator is disabled (disableOpenCL) and this build has no CPU path"
+        std::cerr << where << ": the accelerator is disabled (disableOpenCL) and the drop-in has no CPU path"
                   << std::endl;
         std::abort();
     }

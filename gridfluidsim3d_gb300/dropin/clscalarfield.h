@@ -5,7 +5,7 @@
 // reference's accelerated path does.
 //
 // The device toggles are kept.  "OpenCL enabled" (the default) selects the
-// CUDA backend; disableOpenCL() leaves no backend (this build has no CPU
+// CUDA backend; disableOpenCL() leaves no backend (the drop-in has no CPU
 // path), and the splat methods then abort with a message.
 #ifndef CLSCALARFIELD_H
 #define CLSCALARFIELD_H

@@ -36,7 +36,7 @@ void ParticleAdvector::setKernelWorkLoadSize(int n) { _kernelWorkLoadSize = n; }
 
 void ParticleAdvector::_requireBackend(const char *where) {
     if (!_isOpenCLEnabled) {
-        std::cerr << where << ": the accelerator is disabled (disableOpenCL) and this build has no CPU path"
+        std::cerr << where << ": the accelerator is disabled (disableOpenCL) and the drop-in has no CPU path"
                   << std::endl;
         std::abort();
     }

@@ -4,7 +4,7 @@
 // (gfs_tricubic_interpolate, gfs_advect_particles) instead of OpenCL.
 //
 // The device toggles are kept.  "OpenCL enabled" (the default) selects the
-// CUDA backend; disableOpenCL() leaves no backend (this build has no CPU
+// CUDA backend; disableOpenCL() leaves no backend (the drop-in has no CPU
 // path), and the compute methods then abort with a message.
 #ifndef PARTICLEADVECTOR_H
 #define PARTICLEADVECTOR_H
