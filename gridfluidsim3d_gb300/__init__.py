@@ -9,10 +9,11 @@ does, and there is no CPU fallback.
 from ._lib import GFSError, PRECISION_MIXED, PRECISION_PLAIN  # noqa: F401
 from . import config  # noqa: F401
 from .core import (AIR, FLUID, SOLID, CLScalarField, Context, CuboidFluidSource, FluidSimulation,  # noqa: F401
+                   GridIndex,
                    FluidSimulationSaveState, FluidSource, MACVelocityField, SphericalFluidSource, ParticleAdvector, PressureSolver,
                    PressureSolverParameters, face_shape)
 
 __all__ = ["GFSError", "PRECISION_PLAIN", "PRECISION_MIXED", "AIR", "FLUID", "SOLID", "Context",
            "CLScalarField", "ParticleAdvector", "PressureSolver", "PressureSolverParameters",
            "MACVelocityField", "FluidSimulation", "FluidSimulationSaveState", "FluidSource", "SphericalFluidSource", "CuboidFluidSource",
-           "face_shape", "config"]
+           "GridIndex", "face_shape", "config"]

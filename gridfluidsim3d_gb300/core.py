@@ -49,6 +49,44 @@ def face_shape(d, isize, jsize, ksize):
     return (ksize + (d == 2), jsize + (d == 1), isize + (d == 0))
 
 
+class GridIndex:
+    """A cell index (i, j, k), as pyfluid's GridIndex (pyfluid/gridindex.py):
+    attributes i, j, k, indexable and iterable in that order."""
+
+    __slots__ = ("i", "j", "k")
+
+    def __init__(self, i=0, j=0, k=0):
+        if isinstance(i, GridIndex):
+            i, j, k = i.i, i.j, i.k
+        self.i, self.j, self.k = int(i), int(j), int(k)
+
+    def __getitem__(self, a):
+        if not isinstance(a, int):
+            raise TypeError("index must be an integer")
+        if not 0 <= a <= 2:
+            raise IndexError("index must be in [0, 2]")
+        return (self.i, self.j, self.k)[a]
+
+    def __setitem__(self, a, value):
+        if not isinstance(a, int):
+            raise TypeError("index must be an integer")
+        if not 0 <= a <= 2:
+            raise IndexError("index must be in [0, 2]")
+        setattr(self, "ijk"[a], int(value))
+
+    def __iter__(self):
+        return iter((self.i, self.j, self.k))
+
+    def __eq__(self, other):
+        return isinstance(other, GridIndex) and tuple(self) == tuple(other)
+
+    def __hash__(self):
+        return hash((self.i, self.j, self.k))
+
+    def __repr__(self):
+        return f"GridIndex({self.i}, {self.j}, {self.k})"
+
+
 class Context:
     """One CUDA device and stream (replaces the reference's OpenCL set-up)."""
 

@@ -94,3 +94,18 @@ def test_fluid_cell_index_out_of_range():
     except IndexError:
         return
     raise AssertionError("out-of-range cell accepted")
+
+
+def test_cell_lists_for_the_queues():
+    """FluidSimulation.add_fluid_cells / remove_fluid_cells take pyfluid
+    GridIndex objects or (i, j, k) rows; both become int32 triples."""
+    from gridfluidsim3d_gb300 import FluidSimulation, GridIndex
+    g = [GridIndex(1, 2, 3), GridIndex(GridIndex(4, 5, 6))]
+    a = FluidSimulation._cells(g)
+    b = FluidSimulation._cells([(1, 2, 3), [4, 5, 6]])
+    c = FluidSimulation._cells(np.array([[1, 2, 3], [4, 5, 6]], np.int64))
+    for x in (a, b, c):
+        assert x.dtype == np.int32 and x.flags.c_contiguous
+        assert x.tolist() == [[1, 2, 3], [4, 5, 6]]
+    assert FluidSimulation._cells([]).shape == (0, 3)
+    assert list(g[1]) == [4, 5, 6] and g[1][2] == 6 and g[0] == GridIndex(1, 2, 3)
