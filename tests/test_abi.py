@@ -51,3 +51,15 @@ def test_errors_are_reported_not_raised(lib):
     assert "NULL" in str(e.value)
     with pytest.raises(_lib.GFSError):
         lib.gfs_sim_default_params(None)
+
+
+def test_fluid_cell_queue_arguments(lib):
+    # gfs_sim_add_fluid_cells / gfs_sim_remove_fluid_cells validate before any device work
+    cells = (ctypes.c_int32 * 3)(1, 2, 3)
+    with pytest.raises(_lib.GFSError) as e:
+        lib.gfs_sim_add_fluid_cells(None, cells, 1, None)
+    assert "invalid arguments" in str(e.value)
+    with pytest.raises(_lib.GFSError):
+        lib.gfs_sim_remove_fluid_cells(None, cells, 1)
+    with pytest.raises(_lib.GFSError):
+        lib.gfs_sim_update_fluid_sources(None, None, None)
