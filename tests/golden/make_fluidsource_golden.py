@@ -25,6 +25,10 @@
    removal, the added queue, the removed queue, the sources, classification),
    jitter factor 0, saved with FluidSimulation::saveState.
 
+5. `fluidsource_edge_ref.state` and `fluidsource_edge_sources.json`: the same input
+   with sources across the grid's faces (see EDGE_SOURCES), after the reference's
+   _updateFluidSources, jitter factor 0.
+
 Needs the reference's source tree and g++; the fixtures are committed.
 
     python tests/golden/make_fluidsource_golden.py
@@ -55,6 +59,21 @@ SOURCES = [
     {"shape": "sphere", "position": [1.5, 2.5, 1.5], "radius": 0.5, "velocity": [0.0, 0.0, 0.0], "active": False},
 ]
 
+
+# Sources across the grid's faces, for the clamping branches of fitAABBtoGrid and
+# getGridIndexBounds (grid3d.h:350-371, 426-439, 485-502): a sphere past the far
+# corner, a cuboid starting below zero (fitAABBtoGrid then moves the whole minimum
+# corner to the origin), a cuboid past the far faces, spheres of radius 0 and -1,
+# and an outflow cuboid over the pool's edge.  Written to fluidsource_edge_*.
+EDGE_SOURCES = [
+    {"shape": "sphere", "position": [3.9, 3.4, 2.9], "radius": 0.5, "velocity": [0.0, -1.0, 0.0]},
+    {"shape": "cuboid", "position": [-0.3, 1.8, -0.2], "size": [0.9, 0.6, 0.8], "velocity": [0.5, 0.0, 0.25]},
+    {"shape": "cuboid", "position": [3.2, 2.6, 2.2], "size": [1.5, 1.5, 1.5], "velocity": [-0.5, 0.0, 0.0]},
+    {"shape": "sphere", "position": [2.0, 2.0, 1.5], "radius": 0.0, "velocity": [1.0, 1.0, 1.0]},
+    {"shape": "sphere", "position": [1.0, 2.5, 1.0], "radius": -1.0, "velocity": [1.0, 1.0, 1.0]},
+    {"shape": "cuboid", "position": [0.1, 0.2, 0.1], "size": [1.0, 0.9, 2.9], "velocity": [0.0, 0.0, 0.0],
+     "outflow": True},
+]
 
 # addFluidCells groups (cells, velocity or None for the overload without one) and
 # the removeFluidCells list; (i, j, k) in the 16 x 14 x 12 grid above
@@ -116,8 +135,8 @@ def _probe_queues():
     return body
 
 
-def probe_source(queues=False):
-    body = "".join(_probe_source(q, s) for q, s in enumerate(SOURCES))
+def probe_source(queues=False, sources=SOURCES):
+    body = "".join(_probe_source(q, s) for q, s in enumerate(sources))
     if queues:
         body += _probe_queues()
     update = "sim._updateFluidCells();" if queues else "sim._updateFluidSources();"
@@ -166,15 +185,19 @@ def main():
         json.dump(SOURCES, f, indent=1)
     with open(os.path.join(HERE, "fluidcells_queues.json"), "w") as f:
         json.dump({"added": [{"cells": c, "velocity": v} for c, v in ADD_GROUPS], "removed": REMOVED}, f, indent=1)
+    with open(os.path.join(HERE, "fluidsource_edge_sources.json"), "w") as f:
+        json.dump(EDGE_SOURCES, f, indent=1)
     build.build()
     with tempfile.TemporaryDirectory() as tmp:
         out = os.path.join(tmp, "tree")
         build_reference_tree(SRC, out, opt="-O0")
         lib_dir = os.path.dirname(build.LIB)
-        for queues, dst in ((False, fref), (True, os.path.join(HERE, "fluidcells_ref.state"))):
+        runs = ((False, SOURCES, fref), (True, SOURCES, os.path.join(HERE, "fluidcells_ref.state")),
+                (False, EDGE_SOURCES, os.path.join(HERE, "fluidsource_edge_ref.state")))
+        for queues, sources, dst in runs:
             probe = os.path.join(tmp, "probe.cpp")
             with open(probe, "w") as f:
-                f.write(probe_source(queues))
+                f.write(probe_source(queues, sources))
             exe = os.path.join(tmp, "probe")
             subprocess.run(["g++", "-std=c++11", "-O0", "-w", "-DNFLUIDSIMDEBUG", "-include", "limits", "-I" + out,
                             "-I" + os.path.join(ROOT, "include"), probe, "-o", exe, "-L" + out, "-lfluidsim_gfs",

@@ -109,3 +109,16 @@ def test_cell_lists_for_the_queues():
         assert x.tolist() == [[1, 2, 3], [4, 5, 6]]
     assert FluidSimulation._cells([]).shape == (0, 3)
     assert list(g[1]) == [4, 5, 6] and g[1][2] == 6 and g[0] == GridIndex(1, 2, 3)
+
+
+def test_oracle_matches_reference_edge_sources():
+    """Sources across the grid's faces (tests/golden/fluidsource_edge_sources.json):
+    the clamping of fitAABBtoGrid / getGridIndexBounds, radius 0 and -1, and an
+    outflow over the pool's edge, against the reference's _updateFluidSources."""
+    inp, _, _, mat = load_case()
+    ref = S.read_state(os.path.join(G, "fluidsource_edge_ref.state"))
+    srcs = json.load(open(os.path.join(G, "fluidsource_edge_sources.json")))
+    _, p, v, ids, _ = F.update_fluid_sources(inp["dims"], inp["dx"], mat, inp["positions"], inp["velocities"],
+                                            np.arange(len(inp["positions"])), srcs, jitter_factor=0.0)
+    assert len(p) == len(ref["positions"]) == 3699
+    assert np.array_equal(rows(p, v), rows(ref["positions"], ref["velocities"]))
