@@ -113,6 +113,27 @@ def test_substep_with_sources(gpu_ctx, oracle_lib):
     assert np.abs(gv - rv).max() / max(np.abs(rv).max(), 1.0) < 1e-4
 
 
+def test_edge_sources_match_reference(gpu_ctx):
+    """Sources across the grid's faces (clamped bounds, radius 0 and -1, an outflow
+    over the pool's edge) against the reference's result, jitter 0."""
+    ref = S.read_state(os.path.join(G, "fluidsource_edge_ref.state"))
+    sim = FluidSimulation.from_save_state(FIN, max_particles=8000, ctx=gpu_ctx)
+    sim.set_marker_particle_jitter(0.0)
+    for s in json.load(open(os.path.join(G, "fluidsource_edge_sources.json"))):
+        if s["shape"] == "sphere":
+            src = SphericalFluidSource(s["position"], s["radius"], s["velocity"])
+            src.is_inflow = not s.get("outflow", False)
+            sim.add_spherical_fluid_source(src)
+        else:
+            src = CuboidFluidSource(s["position"], *s["size"], velocity=s["velocity"])
+            src.is_inflow = not s.get("outflow", False)
+            sim.add_cuboid_fluid_source(src)
+    added, removed = sim.update_fluid_sources()
+    pos, vel, _ = sim.get_marker_particles()
+    assert len(pos) == len(ref["positions"]) == 4480 + added - removed
+    assert np.array_equal(rows(pos, vel), rows(ref["positions"], ref["velocities"]))
+
+
 def test_capacity_error(gpu_ctx):
     sim = FluidSimulation.from_save_state(FIN, max_particles=4600, ctx=gpu_ctx)
     with_sources(sim)
