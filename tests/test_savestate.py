@@ -83,3 +83,34 @@ def test_library_header_reader_truncated(tmp_path):
     p.write_bytes(open(FREF, "rb").read()[:20])
     with pytest.raises(GFSError, match="truncated"):
         FluidSimulationSaveState().load_state(str(p))
+
+
+def test_library_header_reader_matches_oracle(tmp_path):
+    """gfs_savestate_read_header (host-only: it opens and parses the file, no
+    device work) through pyfluid's FluidSimulationSaveState, on every committed
+    savestate fixture; a truncated and a missing file fail with GFSError."""
+    import glob
+    import shutil
+
+    if not shutil.which("nvcc") and not os.path.exists("/usr/local/cuda/bin/nvcc"):
+        pytest.skip("no CUDA toolkit")
+    from gridfluidsim3d_gb300 import FluidSimulationSaveState, GFSError, build
+    build.build()
+    files = sorted(glob.glob(os.path.join(HERE, "golden", "*.state")))
+    assert len(files) >= 5
+    for path in files:
+        ref = S.read_state(path)
+        st = FluidSimulationSaveState()
+        assert st.load_state(path)
+        assert st.get_grid_dimensions() == ref["dims"]
+        assert st.get_cell_size() == ref["dx"]
+        assert st.get_current_frame() == ref["frame"]
+        assert st.get_num_marker_particles() == len(ref["positions"])
+        assert st.get_num_diffuse_particles() == len(ref["diffuse_positions"])
+        assert st.get_num_solid_cells() == len(ref["solid_cells"])
+    cut = tmp_path / "cut.state"
+    cut.write_bytes(open(files[0], "rb").read()[:20])
+    with pytest.raises(GFSError, match="truncated"):
+        FluidSimulationSaveState().load_state(str(cut))
+    with pytest.raises(GFSError):
+        FluidSimulationSaveState().load_state(str(tmp_path / "missing.state"))
