@@ -24,6 +24,16 @@ GFS_ERR_TIMEOUT = 4
 GFS_ERR_STATE = 5
 PRECISION_PLAIN = 0
 PRECISION_MIXED = 1
+SWEEP_AUTO = 0
+SWEEP_BLOCK = 1
+SWEEP_CLUSTER_4X2 = 2
+SWEEP_CLUSTER_2X2 = 3
+STAGE_UPDATE_FLUID_CELLS = 1
+STAGE_BODY_FORCES = 6
+STAGE_PRESSURE = 7
+STAGE_APPLY_PRESSURE = 8
+STAGE_EXTRAPOLATE = 9
+STAGE_ALL = 12
 
 _ERR_NAMES = {1: "invalid argument", 2: "CUDA error", 3: "out of device memory",
               4: "wavefront wait timed out", 5: "call out of order"}
@@ -73,6 +83,10 @@ _SIGNATURES = {
     "gfs_ctx_profile_enable": [_P, _I],
     "gfs_ctx_profile_reset": [_P],
     "gfs_ctx_profile_read": [_P, _I, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_D), ctypes.POINTER(_I64)],
+    "gfs_ctx_set_sweep_kernel": [_P, _I],
+    "gfs_ctx_last_sweep_kernel": [_P, ctypes.POINTER(_I)],
+    "gfs_ctx_set_wait_limit": [_P, _I64],
+    "gfs_ctx_inject_wait_timeout": [_P, _I],
     "gfs_scalar_field_add_point_values": [_P, _P, _P, _I64, _D, _P, _D, _I, _I, _I, _P, _P, _I, _D],
     "gfs_velocity_scalar_field": [_P, _I, _I, _I, _I, _D, _P, _P, _I64, _P, _P],
     "gfs_tricubic_interpolate": [_P, _I, _I, _I, _D, _P, _P, _P, _P, _I64, _P],
@@ -94,6 +108,8 @@ _SIGNATURES = {
     "gfs_sim_get_pressure_grid": [_P, _P],
     "gfs_sim_step": [_P, _D, ctypes.POINTER(StepStats)],
     "gfs_sim_step_host": [_P, _D, _P, _P, _P, ctypes.POINTER(_I64), ctypes.POINTER(StepStats)],
+    "gfs_sim_step_stages": [_P, _D, _I, ctypes.POINTER(StepStats)],
+    "gfs_sim_get_saved_velocity_field": [_P, _P, _P, _P],
     "gfs_sim_pressure_check": [_P, _D, _D, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_I)],
     "gfs_sim_set_fluid_sources": [_P, ctypes.POINTER(FluidSourceC), _I],
     "gfs_sim_set_marker_particle_jitter": [_P, _D, ctypes.c_uint64],

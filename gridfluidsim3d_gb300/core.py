@@ -128,6 +128,25 @@ class Context:
         _lib.lib().gfs_ctx_launch_count(self._h, ctypes.byref(c))
         return c.value
 
+    # -- wavefront kernels of the MIC(0) triangular solves (gfs_ctx_set_sweep_kernel) --
+    def set_sweep_kernel(self, kind: int):
+        """SWEEP_AUTO (default), SWEEP_BLOCK, SWEEP_CLUSTER_4X2 or SWEEP_CLUSTER_2X2."""
+        _lib.lib().gfs_ctx_set_sweep_kernel(self._h, int(kind))
+
+    def last_sweep_kernel(self) -> int:
+        k = ctypes.c_int()
+        _lib.lib().gfs_ctx_last_sweep_kernel(self._h, ctypes.byref(k))
+        return k.value
+
+    def set_wait_limit(self, polls: int = 0):
+        """Bound of every wavefront wait in polls (0: the library default)."""
+        _lib.lib().gfs_ctx_set_wait_limit(self._h, int(polls))
+
+    def inject_wait_timeout(self, sweeps: int = 1):
+        """Make the next `sweeps` wavefront launches wait for a tag nobody writes
+        (test hook of the GFS_ERR_TIMEOUT path; every wait ends at its bound)."""
+        _lib.lib().gfs_ctx_inject_wait_timeout(self._h, int(sweeps))
+
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
             _lib.lib().gfs_ctx_destroy(self._h)
@@ -472,6 +491,24 @@ class FluidSimulation:
         out = np.zeros((self.ksize, self.jsize, self.isize), np.float32)
         _lib.lib().gfs_sim_get_pressure_grid(self._h, _p(out))
         return out
+
+    def get_saved_velocity_field(self) -> MACVelocityField:
+        """The last step's saved field (after _advectVelocityField, extrapolated),
+        which the PIC/FLIP update reads as the old velocities."""
+        f = MACVelocityField(self.isize, self.jsize, self.ksize, self.dx)
+        _lib.lib().gfs_sim_get_saved_velocity_field(self._h, _p(f.u), _p(f.v), _p(f.w))
+        return f
+
+    def step_stages(self, dt, last_stage) -> dict:
+        """The substep of update(dt) up to the end of stage `last_stage` of
+        FluidSimulation::_stepFluid (STAGE_UPDATE_FLUID_CELLS, STAGE_BODY_FORCES,
+        STAGE_PRESSURE, STAGE_APPLY_PRESSURE, STAGE_EXTRAPOLATE or STAGE_ALL).
+        Before STAGE_ALL the particles are not advanced and the frame counter
+        does not move."""
+        st = StepStats()
+        _lib.lib().gfs_sim_step_stages(self._h, float(dt), int(last_stage), ctypes.byref(st))
+        self.last_stats = st.as_dict()
+        return self.last_stats
 
     # -- fluid sources (fluidsimulation.cpp:767-810; pyfluid/fluidsimulation.py:626-648) --
     def _push_sources(self):

@@ -201,6 +201,12 @@ extern "C" int gfs_tricubic_interpolate_noalloc(int ni, int nj, int nk, double d
         set_error(GFS_ERR_INVALID, "gfs_tricubic_interpolate_noalloc: invalid arguments");
         return GFS_ERR_INVALID;
     }
+    // the padded extents below are int sums: reject dimensions that could overflow
+    // them before forming any (the scratch bound rejects everything near this anyway)
+    if (ni > (1 << 20) || nj > (1 << 20) || nk > (1 << 20) || (long long)ni * nj * nk >= (1LL << 31)) {
+        set_error(GFS_ERR_INVALID, "gfs_tricubic_interpolate_noalloc: a %d x %d x %d grid is too large", ni, nj, nk);
+        return GFS_ERR_INVALID;
+    }
     Grids g = make_grids(ni, nj, nk, dx);
     unsigned long long need = (unsigned long long)g.f[0].size + g.f[1].size + g.f[2].size;
     if (need > GFS_NOALLOC_SCRATCH_FLOATS) {
@@ -218,8 +224,19 @@ extern "C" int gfs_tricubic_interpolate_noalloc(int ni, int nj, int nk, double d
     }
     float *base = nullptr;
     {
-        // first call on this device (the current one): look up the scratch's device address
+        // first call on this device (the current one): look up the scratch's device
+        // address.  A cached address that the runtime no longer knows as device
+        // memory of this device (the device was reset since, and the library's
+        // module loaded again) is looked up again.
         std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (g_noalloc_base[dev]) {
+            cudaPointerAttributes at{};
+            if (cudaPointerGetAttributes(&at, g_noalloc_base[dev]) != cudaSuccess ||
+                at.type != cudaMemoryTypeDevice || at.device != dev) {
+                cudaGetLastError();
+                g_noalloc_base[dev] = nullptr;
+            }
+        }
         if (!g_noalloc_base[dev]) {
             void *p = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);

@@ -342,49 +342,66 @@ static int sim_get_particles(Sim *s, float *hp, float *hv, uint32_t *hid, int64_
     return GFS_OK;
 }
 
-int sim_step(Sim *s, double dt, gfs_step_stats *stats) {
+int sim_step(Sim *s, double dt, gfs_step_stats *stats, int last_stage) {
     Ctx *ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     if (!(dt >= 0.0) || !std::isfinite(dt)) {
         set_error(GFS_ERR_INVALID, "delta time must be >= 0 (got %g)", dt);
         return GFS_ERR_INVALID;
     }
+    switch (last_stage) {
+    case GFS_STAGE_UPDATE_FLUID_CELLS: case GFS_STAGE_BODY_FORCES: case GFS_STAGE_PRESSURE:
+    case GFS_STAGE_APPLY_PRESSURE: case GFS_STAGE_EXTRAPOLATE: case GFS_STAGE_ALL:
+        break;
+    default:
+        set_error(GFS_ERR_INVALID, "stage %d is not a stop of the substep (1, 6, 7, 8, 9 or 12)", last_stage);
+        return GFS_ERR_INVALID;
+    }
     GFS_CUDA_CHECK(cudaEventRecord(s->ev0, st));
-    int rc = GFS_OK;
-    // stage 1: _updateFluidCells (particle removal happened in the last sort), with
-    // the queued fluid cells and the fluid sources first when there are any
-    // (fluidsimulation.cpp:1990-1994)
-    if (s->need_sort && (rc = sort_particles(s, true))) return rc;
-    if (!s->added_cells.empty() || !s->removed_cells.empty()) {
-        if ((rc = update_fluid_cell_queues(s, nullptr, nullptr))) return rc;
-    }
-    if (!s->sources.empty()) {
-        if ((rc = update_fluid_sources(s, nullptr, nullptr))) return rc;
-    }
-    if (s->need_sort && (rc = sort_particles(s, true))) return rc;
-    if ((rc = classify_cells(s))) return rc;
-    // stage 5: velocity splat, fill, saved field, body forces (stage 6 fused)
-    if ((rc = splat_velocity(s))) return rc;
-    if ((rc = face_fill(s, dt))) return rc;
-    int layers = (int)std::ceil(s->params.cfl + 2.0);
-    if (layers > 120) layers = 120;
-    if ((rc = build_layers(s, layers))) return rc;
-    float *saved[3] = {s->saved[0].as<float>(), s->saved[1].as<float>(), s->saved[2].as<float>()};
-    if ((rc = extrapolate_field(s, saved, layers, false))) return rc;
-    // stage 7: pressure
-    GFS_CUDA_CHECK(cudaEventRecord(s->evp0, st));
-    float *mac[3] = {s->mac[0].as<float>(), s->mac[1].as<float>(), s->mac[2].as<float>()};
     gfs_step_stats local{};
-    rc = pressure_solve(ctx, s->ps, s->g, s->mat.as<uint8_t>(), mac, s->params.density, dt, s->params.precision,
-                        s->params.tol, s->params.max_cg_iterations, &local);
-    if (rc) return rc;
+    int rc = GFS_OK;
+    GFS_CUDA_CHECK(cudaEventRecord(s->evp0, st));
     GFS_CUDA_CHECK(cudaEventRecord(s->evp1, st));
-    // stage 8, 9
-    if ((rc = pressure_apply(s, dt))) return rc;
-    if ((rc = extrapolate_field(s, mac, layers, false))) return rc;
-    // stages 11, 12
-    if ((rc = g2p_advect(s, dt))) return rc;
-    if ((rc = sort_particles(s, true))) return rc;
+    do {
+        // stage 1: _updateFluidCells (particle removal happened in the last sort), with
+        // the queued fluid cells and the fluid sources first when there are any
+        // (fluidsimulation.cpp:1990-1994)
+        if (s->need_sort && (rc = sort_particles(s, true))) return rc;
+        if (!s->added_cells.empty() || !s->removed_cells.empty()) {
+            if ((rc = update_fluid_cell_queues(s, nullptr, nullptr))) return rc;
+        }
+        if (!s->sources.empty()) {
+            if ((rc = update_fluid_sources(s, nullptr, nullptr))) return rc;
+        }
+        if (s->need_sort && (rc = sort_particles(s, true))) return rc;
+        if ((rc = classify_cells(s))) return rc;
+        if (last_stage == GFS_STAGE_UPDATE_FLUID_CELLS) break;
+        // stage 5: velocity splat, fill, saved field, body forces (stage 6 fused)
+        if ((rc = splat_velocity(s))) return rc;
+        if ((rc = face_fill(s, dt))) return rc;
+        int layers = (int)std::ceil(s->params.cfl + 2.0);
+        if (layers > 120) layers = 120;
+        if ((rc = build_layers(s, layers))) return rc;
+        float *saved[3] = {s->saved[0].as<float>(), s->saved[1].as<float>(), s->saved[2].as<float>()};
+        if ((rc = extrapolate_field(s, saved, layers, false))) return rc;
+        if (last_stage == GFS_STAGE_BODY_FORCES) break;
+        // stage 7: pressure
+        GFS_CUDA_CHECK(cudaEventRecord(s->evp0, st));
+        float *mac[3] = {s->mac[0].as<float>(), s->mac[1].as<float>(), s->mac[2].as<float>()};
+        rc = pressure_solve(ctx, s->ps, s->g, s->mat.as<uint8_t>(), mac, s->params.density, dt,
+                            s->params.precision, s->params.tol, s->params.max_cg_iterations, &local);
+        if (rc) return rc;
+        GFS_CUDA_CHECK(cudaEventRecord(s->evp1, st));
+        if (last_stage == GFS_STAGE_PRESSURE) break;
+        // stage 8, 9
+        if ((rc = pressure_apply(s, dt))) return rc;
+        if (last_stage == GFS_STAGE_APPLY_PRESSURE) break;
+        if ((rc = extrapolate_field(s, mac, layers, false))) return rc;
+        if (last_stage == GFS_STAGE_EXTRAPOLATE) break;
+        // stages 11, 12
+        if ((rc = g2p_advect(s, dt))) return rc;
+        if ((rc = sort_particles(s, true))) return rc;
+    } while (false);
     GFS_CUDA_CHECK(cudaEventRecord(s->ev1, st));
     GFS_CUDA_CHECK(cudaEventSynchronize(s->ev1));
     if (ctx->prof.on) ctx->prof.flush();
@@ -485,6 +502,39 @@ int gfs_ctx_launch_count(gfs_ctx *ctx, int64_t *count) {
     GFS_NONNULL(ctx);
     GFS_NONNULL(count);
     *count = ctx->c.launches;
+    return GFS_OK;
+}
+
+int gfs_ctx_set_sweep_kernel(gfs_ctx *ctx, int kind) {
+    GFS_NONNULL(ctx);
+    if (kind < GFS_SWEEP_AUTO || kind > GFS_SWEEP_CLUSTER_2X2) {
+        set_error(GFS_ERR_INVALID, "sweep kernel %d is not one of GFS_SWEEP_AUTO .. GFS_SWEEP_CLUSTER_2X2", kind);
+        return GFS_ERR_INVALID;
+    }
+    ctx->c.sweep_kernel = kind;
+    return GFS_OK;
+}
+
+int gfs_ctx_last_sweep_kernel(gfs_ctx *ctx, int *kind) {
+    GFS_NONNULL(ctx);
+    GFS_NONNULL(kind);
+    *kind = ctx->c.last_sweep_kernel;
+    return GFS_OK;
+}
+
+int gfs_ctx_set_wait_limit(gfs_ctx *ctx, int64_t polls) {
+    GFS_NONNULL(ctx);
+    ctx->c.wait_limit = polls > 0 ? (long long)std::min<int64_t>(polls, (int64_t)1 << 30) : GFS_SPIN_LIMIT;
+    return GFS_OK;
+}
+
+int gfs_ctx_inject_wait_timeout(gfs_ctx *ctx, int sweeps) {
+    GFS_NONNULL(ctx);
+    if (sweeps < 0) {
+        set_error(GFS_ERR_INVALID, "sweeps must be >= 0 (got %d)", sweeps);
+        return GFS_ERR_INVALID;
+    }
+    ctx->c.wait_fault_sweeps = sweeps;
     return GFS_OK;
 }
 
@@ -659,9 +709,27 @@ int gfs_sim_get_pressure_grid(gfs_sim *sim, float *h_pressure) {
     return GFS_OK;
 }
 
+int gfs_sim_get_saved_velocity_field(gfs_sim *sim, float *h_u, float *h_v, float *h_w) {
+    GFS_NONNULL(sim);
+    Sim *s = &sim->s;
+    float *h[3] = {h_u, h_v, h_w};
+    DevMem stage;
+    for (int d = 0; d < 3; d++) {
+        if (!h[d]) continue;
+        int rc = download_padded<float>(s->ctx, s->saved[d].as<float>(), s->g.f[d], h[d], stage);
+        if (rc) return rc;
+    }
+    return GFS_OK;
+}
+
 int gfs_sim_step(gfs_sim *sim, double dt, gfs_step_stats *stats) {
     GFS_NONNULL(sim);
     return sim_step(&sim->s, dt, stats);
+}
+
+int gfs_sim_step_stages(gfs_sim *sim, double dt, int last_stage, gfs_step_stats *stats) {
+    GFS_NONNULL(sim);
+    return sim_step(&sim->s, dt, stats, last_stage);
 }
 
 int gfs_sim_step_host(gfs_sim *sim, double dt, float *h_positions, float *h_velocities, uint32_t *h_ids,

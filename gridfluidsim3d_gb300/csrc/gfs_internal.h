@@ -56,6 +56,14 @@ struct Ctx {
     int64_t launches = 0;
     char device_name[256] = {0};
     Profiler prof;
+    // wavefront kernels of the MIC(0) triangular solves (GFS_SWEEP_*): the one
+    // asked for, and the one the last solve ran
+    int sweep_kernel = GFS_SWEEP_AUTO;
+    int last_sweep_kernel = GFS_SWEEP_AUTO;
+    // bound of every wavefront wait, in polls, and the number of coming sweeps
+    // whose waits look for an exchange tag that no producer writes
+    long long wait_limit = GFS_SPIN_LIMIT;
+    int wait_fault_sweeps = 0;
 };
 
 // Scoped timing of one kernel class (no-op unless the profiler is on).
@@ -158,7 +166,8 @@ int splat_velocity(Sim *s, float *const wsum[3] = nullptr);   // P2G for U, V, W
 int face_fill(Sim *s, double dt);     // a3 + saved copy + body forces
 
 // ---- capi.cu
-int sim_step(Sim *s, double dt, gfs_step_stats *stats);   // one device-resident substep
+// one device-resident substep, or its stages up to last_stage (GFS_STAGE_*)
+int sim_step(Sim *s, double dt, gfs_step_stats *stats, int last_stage = GFS_STAGE_ALL);
 int sim_stage_xyz(Sim *s, int64_t *n_out);   // particles -> xyz triples in pos_alt / vel_alt (ids in key)
 int sim_unstage_xyz(Sim *s, int64_t n);      // n staged triples (ids 0..n-1) -> particles, sorted
 

@@ -299,6 +299,8 @@ struct SweepArgs {
     double *partials;
     PsCtrl *ctrl;
     int init;                // BWD: first solve of a CG run (sets sigma, no beta)
+    int spin_limit;          // bound of every exchange wait, in polls
+    unsigned wait_skew;      // 0; nonzero (fault injection) makes every wait look for a tag nobody writes
 };
 
 // Fluid bits of the neighbours the MIC(0) diagonal needs, packed:
@@ -417,12 +419,12 @@ template <> struct Xch<double> {
 // Take a prefetched exchange word, re-reading it (bounded) until it carries this sweep's tag.
 template <class T>
 __device__ __forceinline__ T xch_take(unsigned long long w[], const unsigned long long *src, unsigned tag,
-                                      PsCtrl *ctrl, bool &timed_out) {
+                                      int limit, PsCtrl *ctrl, bool &timed_out) {
     if (!Xch<T>::ready(w, tag) && !timed_out) {
         int spins = 0;
         do {
             Xch<T>::fetch(src, w);
-            if (++spins > GFS_SPIN_LIMIT) {
+            if (++spins > limit) {
                 atomicOr(&ctrl->err, GFS_DEV_ERR_TIMEOUT);
                 timed_out = true;
                 break;
@@ -510,6 +512,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1) k_sweep(SweepArgs<T> A) {
     }
     __syncthreads();
     const unsigned t = sh_ticket, tag = sh_epoch;
+    const unsigned wtag = tag + A.wait_skew;   // the tag the waits look for (tag itself unless a test skews it)
     int bj = (int)(t % K.nbj), bk = (int)(t / K.nbj);
     if (bwd) {
         bj = K.nbj - 1 - bj;
@@ -610,9 +613,9 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1) k_sweep(SweepArgs<T> A) {
                 const long long o = (long long)st * PS;
                 T nj_, nk_;
                 if (!at_j) nj_ = xb[(st - 1) & 1][kl][xj];
-                else nj_ = in_j ? xch_take<T>(r_wj[v], pxj + (long long)st * XS, tag, A.ctrl, timed_out) : T(0);
+                else nj_ = in_j ? xch_take<T>(r_wj[v], pxj + (long long)st * XS, wtag, A.spin_limit, A.ctrl, timed_out) : T(0);
                 if (!at_k) nk_ = xb[(st - 1) & 1][xk][jl];
-                else nk_ = in_k ? xch_take<T>(r_wk[v], pxk + (long long)st * XS, tag, A.ctrl, timed_out) : T(0);
+                else nk_ = in_k ? xch_take<T>(r_wk[v], pxk + (long long)st * XS, wtag, A.spin_limit, A.ctrl, timed_out) : T(0);
                 T val = T(0);
                 if (MODE == SW_FWD) {
                     // _applyPreconditioner forward solve (pressuresolver.cpp:311-351); neighbours hand
@@ -720,6 +723,7 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
     }
     __syncthreads();
     const unsigned t = sh_ticket, tag = sh_epoch;
+    const unsigned wtag = tag + A.wait_skew;   // the tag the waits look for (tag itself unless a test skews it)
     int bj = (int)(t % K.nbj), bk = (int)(t / K.nbj);
     if (bwd) {
         bj = K.nbj - 1 - bj;
@@ -819,8 +823,8 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
             const bool act = st >= st_lo && st < st_hi;
             T nj_ = at_j ? T(0) : xb[(st - 1) & 1][kl][xj];
             T nk_ = at_k ? T(0) : xb[(st - 1) & 1][xk][jl];
-            if (in_j && act) nj_ = xch_take<T>(r_wj[v], pxj_in + (long long)st * XS, tag, A.ctrl, timed_out);
-            if (in_k && act) nk_ = xch_take<T>(r_wk[v], pxk_in + (long long)st * XS, tag, A.ctrl, timed_out);
+            if (in_j && act) nj_ = xch_take<T>(r_wj[v], pxj_in + (long long)st * XS, wtag, A.spin_limit, A.ctrl, timed_out);
+            if (in_k && act) nk_ = xch_take<T>(r_wk[v], pxk_in + (long long)st * XS, wtag, A.spin_limit, A.ctrl, timed_out);
             const T ra = ring[0][u][tid], pc = ring[1][u][tid];
             T val, xch;
             if (MODE == SW_FWD) {
@@ -914,7 +918,8 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
 // resident while its peers may still store into it.  Arithmetic, summation
 // order and outputs are k_tri's.
 template <class T>
-__device__ __forceinline__ T rx_take(const unsigned long long *p, unsigned tag, PsCtrl *ctrl, bool &timed_out) {
+__device__ __forceinline__ T rx_take(const unsigned long long *p, unsigned tag, int limit, PsCtrl *ctrl,
+                                     bool &timed_out) {
     using X = Xch<T>;
     unsigned long long w[X::W];
 #pragma unroll
@@ -924,7 +929,7 @@ __device__ __forceinline__ T rx_take(const unsigned long long *p, unsigned tag, 
         do {
 #pragma unroll
             for (int q = 0; q < X::W; q++) w[q] = *(const volatile unsigned long long *)(p + q);
-            if (++spins > GFS_SPIN_LIMIT) {
+            if (++spins > limit) {
                 atomicOr(&ctrl->err, GFS_DEV_ERR_TIMEOUT);
                 timed_out = true;
                 break;
@@ -981,6 +986,7 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE, 1)
     }
     cl.sync();
     const unsigned t = *cl.map_shared_rank(&sh_ticket, 0u), tag = sh_epoch;
+    const unsigned wtag = tag + A.wait_skew;
     const int ncj = (K.nbj + CL_J - 1) / CL_J, nck = (K.nbk + CL_K - 1) / CL_K;
     int cj = (int)(t % (unsigned)ncj), ck = (int)(t / (unsigned)ncj);
     if (bwd) {
@@ -1094,11 +1100,11 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE, 1)
             T nj_ = at_j ? T(0) : xb[(st - 1) & 1][kl][xj];
             T nk_ = at_k ? T(0) : xb[(st - 1) & 1][xk][jl];
             if (in_j && act)
-                nj_ = pj_cl ? rx_take<T>(rj_in + (long long)st * SBK * W, tag, A.ctrl, timed_out)
-                            : xch_take<T>(r_wj[v], pxj_in + (long long)st * XS, tag, A.ctrl, timed_out);
+                nj_ = pj_cl ? rx_take<T>(rj_in + (long long)st * SBK * W, wtag, A.spin_limit, A.ctrl, timed_out)
+                            : xch_take<T>(r_wj[v], pxj_in + (long long)st * XS, wtag, A.spin_limit, A.ctrl, timed_out);
             if (in_k && act)
-                nk_ = pk_cl ? rx_take<T>(rk_in + (long long)st * SBJ * W, tag, A.ctrl, timed_out)
-                            : xch_take<T>(r_wk[v], pxk_in + (long long)st * XS, tag, A.ctrl, timed_out);
+                nk_ = pk_cl ? rx_take<T>(rk_in + (long long)st * SBJ * W, wtag, A.spin_limit, A.ctrl, timed_out)
+                            : xch_take<T>(r_wk[v], pxk_in + (long long)st * XS, wtag, A.spin_limit, A.ctrl, timed_out);
             const T ra = ring[0][u][tid], pc = ring[1][u][tid];
             T val, xch;
             if (MODE == SW_FWD) {
@@ -1608,16 +1614,6 @@ static int ensure_ws(Ctx *ctx, PressureWs &ws, const Grids &g, bool mixed) {
     return GFS_OK;
 }
 
-// The clustered triangular solves run unless GFS_SWEEP_CLUSTER=0 is set in the
-// environment when the library first solves (then k_tri runs everywhere).
-static bool sweep_cluster_enabled() {
-    static const bool on = [] {
-        const char *e = getenv("GFS_SWEEP_CLUSTER");
-        return !(e && e[0] == '0');
-    }();
-    return on;
-}
-
 // k_tri_cl<.., CJ, CK> fits when its receive buffers fit in shared memory and
 // every cluster of the launch can be resident at once (a cluster that waits for
 // a free SM would serialise the wavefront); checked, and the shared-memory
@@ -1709,13 +1705,35 @@ static int launch_sweep(Ctx *ctx, PressureWs &ws, const T *in, T *out, const T *
     A.partials = ws.partials.as<double>();
     A.ctrl = C;
     A.init = init;
+    A.spin_limit = (int)ctx->wait_limit;
+    A.wait_skew = 0u;
+    if (ctx->wait_fault_sweeps > 0) {
+        A.wait_skew = 0x40000000u;
+        ctx->wait_fault_sweeps--;
+    }
     ProfScope prof(ctx, MODE == SW_FWD ? KC_SWEEP_FWD : (MODE == SW_BWD ? KC_SWEEP_BWD : KC_PRECON));
-    // the build runs k_sweep, the triangular solves k_tri (only the launched kernel is instantiated)
-    if constexpr (MODE == SW_PRECON)
+    // the build runs k_sweep, the triangular solves the context's kernel (only the
+    // launched kernels are instantiated)
+    if constexpr (MODE == SW_PRECON) {
         k_sweep<T, MODE, P, PE><<<A.K.nbj * A.K.nbk, SWEEP_THREADS, 0, ctx->stream>>>(A);
-    else if (!(sweep_cluster_enabled() && (launch_tri_cl<T, MODE, P, PE, 4, 2>(ctx, A) ||
-                                           launch_tri_cl<T, MODE, P, PE, 2, 2>(ctx, A))))
-        k_tri<T, MODE, P, PE><<<A.K.nbj * A.K.nbk, SPLANE, 0, ctx->stream>>>(A);
+    } else {
+        const int want = ctx->sweep_kernel;
+        int ran = 0;
+        if ((want == GFS_SWEEP_AUTO || want == GFS_SWEEP_CLUSTER_4X2) && launch_tri_cl<T, MODE, P, PE, 4, 2>(ctx, A))
+            ran = GFS_SWEEP_CLUSTER_4X2;
+        else if ((want == GFS_SWEEP_AUTO || want == GFS_SWEEP_CLUSTER_2X2) &&
+                 launch_tri_cl<T, MODE, P, PE, 2, 2>(ctx, A))
+            ran = GFS_SWEEP_CLUSTER_2X2;
+        else if (want == GFS_SWEEP_AUTO || want == GFS_SWEEP_BLOCK) {
+            k_tri<T, MODE, P, PE><<<A.K.nbj * A.K.nbk, SPLANE, 0, ctx->stream>>>(A);
+            ran = GFS_SWEEP_BLOCK;
+        } else {
+            set_error(GFS_ERR_INVALID, "sweep kernel %d cannot run this %dx%dx%d solve: its clusters do not all "
+                      "fit on the device at once", want, A.K.nx, A.K.ny, A.K.nz);
+            return GFS_ERR_INVALID;
+        }
+        ctx->last_sweep_kernel = ran;
+    }
     ctx->launches++;
     GFS_LAUNCH_CHECK();
     return GFS_OK;

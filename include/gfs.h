@@ -135,6 +135,9 @@ int gfs_advect_particles(gfs_ctx *ctx, int order, int ni, int nj, int nk, double
    faces need more than 12,582,912 floats (about 150^3 cells) are rejected with
    GFS_ERR_INVALID.  The first call on a device (the current device) looks up the
    scratch's device address; make that first call before any stream capture.
+   Every call checks the cached address with cudaPointerGetAttributes; after a
+   cudaDeviceReset, which unloads the scratch, the first call looks it up again
+   (make that call before any stream capture too).
    All calls share the scratch: calls that overlap on the GPU race on it.  The
    call is asynchronous; results are ready when `stream` has been synchronised. */
 int gfs_tricubic_interpolate_noalloc(int ni, int nj, int nk, double dx, const float *d_u,
@@ -230,6 +233,34 @@ int gfs_sim_step(gfs_sim *sim, double dt, gfs_step_stats *stats);
    input count. */
 int gfs_sim_step_host(gfs_sim *sim, double dt, float *h_positions, float *h_velocities,
                       uint32_t *h_ids, int64_t *n, gfs_step_stats *stats);
+
+/* The substep of gfs_sim_step run only up to the end of one of its stages,
+   numbered as FluidSimulation::_stepFluid numbers them (fluidsimulation.cpp:
+   3262-3390), so that each stage's grids can be read and compared with the
+   reference's:
+     GFS_STAGE_UPDATE_FLUID_CELLS (1)  _updateFluidCells
+     GFS_STAGE_BODY_FORCES        (6)  + _advectVelocityField, the saved field
+                                         and its extrapolation, body forces
+                                         (the splat/fill and the body force are
+                                         one kernel here, so 5 alone is not a stop)
+     GFS_STAGE_PRESSURE           (7)  + _updatePressureGrid
+     GFS_STAGE_APPLY_PRESSURE     (8)  + _applyPressureToVelocityField
+     GFS_STAGE_EXTRAPOLATE        (9)  + _extrapolateFluidVelocities
+     GFS_STAGE_ALL               (12)  the whole substep (= gfs_sim_step)
+   Before GFS_STAGE_ALL the particles are not advanced: a later gfs_sim_step
+   runs the whole substep from the same particles.  Other values fail with
+   GFS_ERR_INVALID. */
+#define GFS_STAGE_UPDATE_FLUID_CELLS 1
+#define GFS_STAGE_BODY_FORCES 6
+#define GFS_STAGE_PRESSURE 7
+#define GFS_STAGE_APPLY_PRESSURE 8
+#define GFS_STAGE_EXTRAPOLATE 9
+#define GFS_STAGE_ALL 12
+int gfs_sim_step_stages(gfs_sim *sim, double dt, int last_stage, gfs_step_stats *stats);
+/* The saved field of the last (partial) step: the velocity field after
+   _advectVelocityField, extrapolated (FluidSimulation::_savedVelocityField,
+   fluidsimulation.cpp:3306-3307), which the PIC/FLIP update reads. */
+int gfs_sim_get_saved_velocity_field(gfs_sim *sim, float *h_u, float *h_v, float *h_w);
 
 /* Accuracy of the last step's pressure solve against FP64: the same system
    (matrix and right-hand side of that step, dt its step length) is solved again
@@ -365,6 +396,41 @@ int gfs_diff_info(gfs_diff *d, double *forward_ms, double *backward_ms, int64_t 
 /* Number of kernel launches the library has issued on this context (for
    accounting in benchmarks). */
 int gfs_ctx_launch_count(gfs_ctx *ctx, int64_t *count);
+
+/* ------------------------------------------ wavefront kernels of the solve */
+
+/* The MIC(0) triangular solves (PressureSolver::_applyPreconditioner,
+   pressuresolver.cpp:304-386) run as i+j+k hyperplane wavefronts over blocks
+   of 16 x 16 pencils.  Three kernels compute the same values in the same order:
+   BLOCK hands block-edge values over through L2 words; CLUSTER_4X2 / _2X2
+   group 4 x 2 or 2 x 2 blocks into a thread-block cluster whose blocks hand
+   over through distributed shared memory.  AUTO (the default) runs the largest
+   cluster shape whose clusters can all be resident on the device, else BLOCK.
+   A cluster shape set explicitly that cannot run on a grid makes the solve fail
+   with GFS_ERR_INVALID.  The preconditioner build always runs its own kernel.
+   No counterpart in the reference (its solves are sequential loops). */
+#define GFS_SWEEP_AUTO 0
+#define GFS_SWEEP_BLOCK 1
+#define GFS_SWEEP_CLUSTER_4X2 2
+#define GFS_SWEEP_CLUSTER_2X2 3
+int gfs_ctx_set_sweep_kernel(gfs_ctx *ctx, int kind);
+/* The kernel the context's last triangular solve ran (GFS_SWEEP_BLOCK /
+   _CLUSTER_4X2 / _CLUSTER_2X2; GFS_SWEEP_AUTO before the first solve). */
+int gfs_ctx_last_sweep_kernel(gfs_ctx *ctx, int *kind);
+
+/* Bound of every wait of the wavefront kernels, in polls of the awaited word
+   (default 4,194,304).  A wait that reaches it sets a device error bit, stops
+   waiting and lets its kernel run to the end; the solve then fails with
+   GFS_ERR_TIMEOUT and the context stays usable (the next solve starts clean).
+   polls <= 0 restores the default.  The reference has no device waits; its
+   failure path is the int *err + message of its C bindings (cbindings.h:25-135),
+   which GFS_ERR_TIMEOUT and gfs_last_error() keep. */
+int gfs_ctx_set_wait_limit(gfs_ctx *ctx, int64_t polls);
+/* Fault injection for tests of that path: the next `sweeps` wavefront launches
+   on this context wait for an exchange tag that no producer writes, so every
+   waiting thread runs into the wait limit (set a small one first).  Nothing
+   faults or hangs: each wait ends at its bound. */
+int gfs_ctx_inject_wait_timeout(gfs_ctx *ctx, int sweeps);
 
 /* Optional per-kernel-class timing with CUDA events recorded on the context's
    stream around every launch (the reference logs stage times with StopWatch,

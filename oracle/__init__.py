@@ -22,9 +22,20 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libgfsoracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libgfsref.so")
-REF_SRC = "/root/reference/src"
+# The reference's src/ directory is found through $GFS_REFERENCE_SRC, or the
+# directory the last build(ref_src=...) recorded in the git-ignored _ref/.
+REF_ENV = "GFS_REFERENCE_SRC"
+REF_RECORD = os.path.join(HERE, "_ref", "reference_src.txt")
 
 AIR, FLUID, SOLID = 0, 1, 2
+
+
+def reference_src() -> str | None:
+    """The reference's src/ directory, or None where it is not available."""
+    p = os.environ.get(REF_ENV, "")
+    if not p and os.path.exists(REF_RECORD):
+        p = open(REF_RECORD).read().strip()
+    return p if p and os.path.isfile(os.path.join(p, "pressuresolver.cpp")) else None
 
 _lib = None
 _ref = None
@@ -44,13 +55,21 @@ class SubstepStats(ctypes.Structure):
                 ("cg_iterations", ctypes.c_int), ("cg_max_resid", ctypes.c_double)]
 
 
-def build(ref: bool | None = None) -> None:
-    """Compile the restatement (and, when the reference tree exists, the shim)."""
+def build(ref: bool | None = None, ref_src: str | None = None) -> None:
+    """Compile the restatement and, when the reference's src/ is known (ref_src,
+    recorded for later runs, or reference_src()), the shim over its sources."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    if ref_src and os.path.isfile(os.path.join(ref_src, "pressuresolver.cpp")):
+        os.makedirs(os.path.dirname(REF_RECORD), exist_ok=True)
+        with open(REF_RECORD, "w") as f:
+            f.write(os.path.abspath(ref_src) + "\n")
+    src = reference_src()
     if ref is None:
-        ref = os.path.isdir(REF_SRC)
+        ref = src is not None
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        if src is None:
+            raise RuntimeError(f"the reference's src/ directory is unknown: set {REF_ENV}")
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={src}"], check=True)
 
 
 def lib():
@@ -95,7 +114,7 @@ def lib():
 
 
 def ref_available() -> bool:
-    return os.path.exists(REF_PATH) or os.path.isdir(REF_SRC)
+    return os.path.exists(REF_PATH) or reference_src() is not None
 
 
 def ref():

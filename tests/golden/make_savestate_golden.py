@@ -25,9 +25,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
+from oracle import reference_src  # noqa: E402
 from oracle import savestate as S  # noqa: E402
 
-SRC = "/root/reference/src"
+SRC = reference_src()   # $GFS_REFERENCE_SRC, or the directory the last oracle build recorded
 DIMS = (12, 10, 9)
 DX = 0.25
 FRAME = 7
@@ -65,6 +66,8 @@ def scene(seed=91):
 
 
 def main():
+    if SRC is None:
+        sys.exit("the reference's src/ directory is unknown: set GFS_REFERENCE_SRC")
     from gridfluidsim3d_gb300 import build
     from gridfluidsim3d_gb300.dropin import build_reference_tree
     mat, pos, vel = scene()

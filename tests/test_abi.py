@@ -63,3 +63,15 @@ def test_fluid_cell_queue_arguments(lib):
         lib.gfs_sim_remove_fluid_cells(None, cells, 1)
     with pytest.raises(_lib.GFSError):
         lib.gfs_sim_update_fluid_sources(None, None, None)
+
+
+def test_noalloc_rejects_overflowing_dims_before_any_device_work(lib):
+    # dims whose padded extents would overflow int are rejected before the grids
+    # are formed; dummy non-NULL pointers are never dereferenced on this path
+    dummy = ctypes.c_void_p(16)
+    big = 2 ** 31 - 4
+    for dims in ((big, big, 1), (1, big, 1), (70000, 70000, 1)):
+        with pytest.raises(_lib.GFSError) as e:
+            lib.gfs_tricubic_interpolate_noalloc(*dims, 0.1, dummy, dummy, dummy, dummy, 1, dummy, None)
+        assert e.value.code == _lib.GFS_ERR_INVALID
+        assert "too large" in str(e.value) or "scratch" in str(e.value)

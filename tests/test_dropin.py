@@ -11,9 +11,11 @@ import subprocess
 
 import pytest
 
-SRC = "/root/reference/src"
+from oracle import reference_src
 
-pytestmark = pytest.mark.skipif(not os.path.isdir(SRC) or not shutil.which("g++"),
+SRC = reference_src()   # $GFS_REFERENCE_SRC, or the directory the last oracle build recorded
+
+pytestmark = pytest.mark.skipif(SRC is None or not shutil.which("g++"),
                                 reason="reference tree or g++ not present")
 
 PROBE = r'''

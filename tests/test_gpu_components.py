@@ -18,9 +18,21 @@ import numpy as np
 import pytest
 
 from gridfluidsim3d_gb300 import (CLScalarField, MACVelocityField, ParticleAdvector, PressureSolver,
-                                  PressureSolverParameters, PRECISION_MIXED, PRECISION_PLAIN, scenes)
+                                  PressureSolverParameters, PRECISION_MIXED, PRECISION_PLAIN, SWEEP_AUTO,
+                                  SWEEP_BLOCK, SWEEP_CLUSTER_2X2, SWEEP_CLUSTER_4X2, scenes)
 
 pytestmark = pytest.mark.gpu
+
+SWEEP_KERNELS = {"block": SWEEP_BLOCK, "cluster4x2": SWEEP_CLUSTER_4X2, "cluster2x2": SWEEP_CLUSTER_2X2}
+
+
+@pytest.fixture(params=list(SWEEP_KERNELS))
+def sweep_ctx(request, gpu_ctx):
+    """The context with each wavefront kernel of the MIC(0) triangular solves in turn
+    (block kernel, 4 x 2 and 2 x 2 clusters); every pressure test runs on all three."""
+    gpu_ctx.set_sweep_kernel(SWEEP_KERNELS[request.param])
+    yield gpu_ctx
+    gpu_ctx.set_sweep_kernel(SWEEP_AUTO)
 
 
 def _fluid_state(O, sc):
@@ -176,12 +188,12 @@ def test_rk_advection(gpu_ctx, oracle_lib, order):
 
 
 @pytest.mark.parametrize("seed,dims", [(0, (16, 12, 14)), (2, (30, 22, 26))])
-def test_pressure_plain_matches_oracle(gpu_ctx, oracle_lib, seed, dims):
+def test_pressure_plain_matches_oracle(sweep_ctx, oracle_lib, seed, dims):
     O = oracle_lib
     sc = scenes.random_box(dims=dims, seed=seed)
     mat, pos, vel, (u, v, w) = _fluid_state(O, sc)
     want, it_ref, res_ref = O.pressure_solve(sc.dims, sc.dx, 20.0, sc.dt, mat, u, v, w)
-    solver = PressureSolver(gpu_ctx, precision=PRECISION_PLAIN)
+    solver = PressureSolver(sweep_ctx, precision=PRECISION_PLAIN)
     got = solver.solve(PressureSolverParameters(sc.dx, 20.0, sc.dt, mat,
                                                 MACVelocityField(*sc.dims, sc.dx, u, v, w)))
     assert abs(solver.iterations - it_ref) <= 1, (solver.iterations, it_ref)
@@ -204,13 +216,13 @@ def _sparse_fluid(dims, seed):
 
 
 @pytest.mark.parametrize("precision", [PRECISION_PLAIN, PRECISION_MIXED])
-def test_pressure_blocks_without_fluid(gpu_ctx, oracle_lib, precision):
+def test_pressure_blocks_without_fluid(sweep_ctx, oracle_lib, precision):
     O = oracle_lib
     dims = (24, 60, 50)
     mat, f = _sparse_fluid(dims, 11)
     dt = 1.0 / 30.0
     want, it_ref, _ = O.pressure_solve(dims, 0.1, 20.0, dt, mat, f.u, f.v, f.w)
-    solver = PressureSolver(gpu_ctx, precision=precision)
+    solver = PressureSolver(sweep_ctx, precision=precision)
     got = solver.solve(PressureSolverParameters(0.1, 20.0, dt, mat, f))
     if precision == PRECISION_PLAIN:
         assert abs(solver.iterations - it_ref) <= 1, (solver.iterations, it_ref)
@@ -219,12 +231,12 @@ def test_pressure_blocks_without_fluid(gpu_ctx, oracle_lib, precision):
     assert res < 1e-6 or it_ref == 200, res
 
 
-def test_pressure_mixed_reaches_tolerance(gpu_ctx, oracle_lib):
+def test_pressure_mixed_reaches_tolerance(sweep_ctx, oracle_lib):
     O = oracle_lib
     sc = scenes.random_box(dims=(30, 22, 26), seed=2)
     mat, pos, vel, (u, v, w) = _fluid_state(O, sc)
     want, it_ref, _ = O.pressure_solve(sc.dims, sc.dx, 20.0, sc.dt, mat, u, v, w, tol=1e-12, max_iters=2000)
-    solver = PressureSolver(gpu_ctx, precision=PRECISION_MIXED)
+    solver = PressureSolver(sweep_ctx, precision=PRECISION_MIXED)
     got = solver.solve(PressureSolverParameters(sc.dx, 20.0, sc.dt, mat,
                                                 MACVelocityField(*sc.dims, sc.dx, u, v, w)))
     assert solver.max_residual < 1e-6
@@ -233,11 +245,11 @@ def test_pressure_mixed_reaches_tolerance(gpu_ctx, oracle_lib):
     assert np.abs(got - want).max() / np.abs(want).max() < 1e-5
 
 
-def test_pressure_no_fluid_and_quiet(gpu_ctx, oracle_lib):
+def test_pressure_no_fluid_and_quiet(sweep_ctx, oracle_lib):
     dims, dx = (10, 9, 8), 0.25
     mat = scenes.solid_border(dims)
     f = MACVelocityField(*dims, dx)
-    solver = PressureSolver(gpu_ctx)
+    solver = PressureSolver(sweep_ctx)
     p = solver.solve(PressureSolverParameters(dx, 20.0, 1 / 30., mat, f))
     assert p.size == 0
     mat[3:6, 3:6, 3:6] = 1

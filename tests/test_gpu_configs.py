@@ -1,0 +1,91 @@
+"""GPU parity on the benchmark configurations, substep by substep.
+
+* Ball drop (the reference's hello-world scene): 64^3 grid, dx = 0.125, solid
+  box walls, a fluid sphere of radius 1.6 centred at (4, 4, 4), 8 particles per
+  fluid cell uniform in-cell from seed 1, zero initial velocity, gravity
+  (0, -25, 0), FLIP ratio 0.95, 30 substeps of 1/30 s (one per frame: the
+  reference's CFL limit never binds, fluidsimulation.cpp:3392-3451); PLAIN
+  (FP64 PCG, the reference's form) and MIXED.
+* Dam break: 128^3 grid, dx = 0.0625, fluid box x < 0.35 L, y < 0.6 L, full z,
+  8 particles per cell from seed 2; two substeps in each form.
+
+The device runs free.  Before each of its substeps the oracle (the C
+restatement of the reference's CPU substep) is given the device's particles
+and runs the same substep; the device's result must then match, particles by
+id.  This is the per-substep error the contract asks for:
+  * identical particle set and fluid-cell classification,
+  * positions within 1e-5 of a cell,
+  * velocities within 1e-4 of the scene's velocity scale,
+  * PLAIN: CG iterations within +-1 of the oracle's.
+"""
+import numpy as np
+import pytest
+
+from gridfluidsim3d_gb300 import FluidSimulation, PRECISION_MIXED, PRECISION_PLAIN, scenes
+
+pytestmark = pytest.mark.gpu
+
+POS_BAR = 1e-5      # cells
+VEL_BAR = 1e-4      # of the velocity scale
+
+
+def _by_id(pos, vel, ids):
+    o = np.argsort(ids, kind="stable")
+    return pos[o], vel[o], ids[o]
+
+
+def _check(step, sc, gstats, gmat, g, o, precision):
+    gpos, gvel, gids = _by_id(*g)
+    opos, ovel, oids = _by_id(o["pos"], o["vel"], o["ids"])
+    assert np.array_equal(gids, oids), f"substep {step}: particle sets differ"
+    assert np.array_equal(gmat, o["mat"]), f"substep {step}: fluid classification differs"
+    assert gstats["num_fluid_cells"] == o["num_fluid_cells"]
+    err = float(np.abs(gpos - opos).max() / sc.dx) if len(gids) else 0.0
+    assert err < POS_BAR, (step, err)
+    vscale = max(float(np.abs(ovel).max()), 1e-3)
+    verr = float(np.abs(gvel - ovel).max() / vscale) if len(gids) else 0.0
+    assert verr < VEL_BAR, (step, verr)
+    if precision == PRECISION_PLAIN:
+        assert abs(gstats["cg_iterations"] - o["cg_iterations"]) <= 1, (step, gstats["cg_iterations"],
+                                                                        o["cg_iterations"])
+    else:
+        assert gstats["cg_max_residual"] < 1e-6 or o["cg_iterations"] < 0, (step, gstats["cg_max_residual"])
+    return err
+
+
+def _run(ctx, O, sc, steps, precision):
+    sim = FluidSimulation(*sc.dims, sc.dx, max_particles=sc.num_particles, ctx=ctx)
+    sim.precision = precision
+    sim.set_material_grid(sc.mat)
+    sim.set_marker_particles(sc.pos, sc.vel, sc.ids)
+    errs, solves = [], 0
+    for step in range(1, steps + 1):
+        pos, vel, ids = sim.get_marker_particles()
+        gstats = sim.update(sc.dt)
+        o = O.substep(sc.dims, sc.dx, sc.dt, sc.gravity, sc.mat, pos, vel, ids)
+        errs.append(_check(step, sc, gstats, sim.get_material_grid(), sim.get_marker_particles(), o, precision))
+        solves += o["cg_iterations"] > 0
+    sim.close()
+    return errs, solves
+
+
+@pytest.mark.parametrize("precision", [PRECISION_PLAIN, PRECISION_MIXED], ids=["plain", "mixed"])
+def test_ball_drop_64_thirty_substeps(gpu_ctx, oracle_lib, precision):
+    sc = scenes.ball_drop(n=64, dx=0.125, seed=1)
+    assert sc.dims == (64, 64, 64) and sc.num_particles > 60000
+    errs, solves = _run(gpu_ctx, oracle_lib, sc, 30, precision)
+    # the sphere falls freely (uniform velocity, no pressure solve) until it meets
+    # the floor; the splash must be inside the checked substeps
+    assert solves >= 5, solves
+    print(f"ball drop 64^3 {['plain', 'mixed'][precision]}: max per-substep position error "
+          f"{max(errs):.2e} cells over 30 substeps, {solves} pressure solves")
+
+
+@pytest.mark.parametrize("precision", [PRECISION_PLAIN, PRECISION_MIXED], ids=["plain", "mixed"])
+def test_dam_break_128_two_substeps(gpu_ctx, oracle_lib, precision):
+    sc = scenes.dam_break(n=128, dx=0.0625, seed=2)
+    assert sc.dims == (128, 128, 128) and sc.num_particles > 3_000_000
+    errs, solves = _run(gpu_ctx, oracle_lib, sc, 2, precision)
+    assert solves == 2
+    print(f"dam break 128^3 {['plain', 'mixed'][precision]}: per-substep position errors "
+          f"{[f'{e:.2e}' for e in errs]} cells")
