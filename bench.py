@@ -24,6 +24,12 @@ cpu_baseline  the oracle (C restatement of the reference's CPU path, single
 accuracy_vs_fp64  per timed substep (re-run untimed): max|p - p_ref| / max|p_ref|
            against an FP64 PCG solve of the same system to 1e-12, and the FP64
            residual max|b - A p| of the step's pressure, for both forms.
+oracle_check  one substep (untimed) against the oracle: the PLAIN pressure against
+           its FP64 PCG (iterations), the MIXED pressure against it solved to 1e-10,
+           and a 400k-particle sample of the PIC/FLIP + RK4 pass recomputed from
+           the device's own grids (per-substep position error in cells).
+configs    the 64^3 ball drop (30 substeps) and the 128^3 dam break (60
+           substeps), both pressure forms, timed on the device.
 savestate  FluidSimulationSaveState write / read of the whole state (GB/s), with the
            oracle's CPU writer beside it.
 fluid_sources  ms per _updateFluidSources call on the 256^3 state (inflow sphere,
@@ -32,7 +38,9 @@ adjoint    fwd+adjoint ms/substep and peak HBM of the two differentiable
            configurations (32^3 cube, 20 substeps, MAC-field parameters; 128^3
            dam break, 60 substeps, per-particle velocities, Adam steps).
 
---impl reference times that CPU path alone and prints its own line.
+--impl reference times one whole substep of the workload on the host cores
+(the oracle stage by stage on the full state, the particle stages on all cores,
+the pressure solve to the reference's rule) and prints its own line.
 --gpus N (under torchrun): N independent replicas (the exact MIC(0)
 preconditioner does not partition), value = total substeps / max time.
 """
@@ -232,31 +240,191 @@ def cpu_estimate(sc, iters, sample_particles=400_000, seed=0):
     return total, parts, time.perf_counter() - t_all, len(sel), n
 
 
+# ------------------------------------------------ measured CPU substep (reference arm)
+#
+# One whole substep of the 256^3 workload on the host cores, every stage on the
+# full state: the oracle (the C restatement of the reference's CPU path) run
+# stage by stage.  The per-particle stages (the velocity splat and the PIC/FLIP +
+# RK4 + collision pass) are split over worker processes (spawned, sharing the
+# particle arrays and grids through shared memory): the splat by k-slabs of the
+# cell-ordered particles into slab grids that the parent adds up, the G2P pass
+# by particle ranges.  The grid-wide stages and the pressure solve run on one
+# core, as the reference runs them (its MIC(0) solves are sequential
+# recurrences); the solve runs to the reference's rule (max|r| < 1e-6, cap 200)
+# on the real system, so its iteration count is measured, not assumed.
+
+_WORKER = {}
+
+
+def _worker_init(spec):
+    from multiprocessing import shared_memory
+    import oracle
+    oracle.lib()
+    _WORKER["O"] = oracle
+    _WORKER["shm"] = [shared_memory.SharedMemory(name=nm) for nm, _, _ in spec.values()]
+    _WORKER["arr"] = {k: np.ndarray(shape, dtype=np.dtype(dt), buffer=sh.buf)
+                      for (k, (nm, shape, dt)), sh in zip(spec.items(), _WORKER["shm"])}
+
+
+def _face_dims(d, dims):
+    ni, nj, nk = dims
+    return ni + (d == 0), nj + (d == 1), nk + (d == 2)
+
+
+def _splat_slab(task):
+    """Splat of particles [a, b) (cells k0..k1-1) into slab grids of the three
+    components: value and weight sums of ScalarField::addPointValue, radius dx."""
+    a, b, k0, k1, dims, dx = task
+    O, A = _WORKER["O"], _WORKER["arr"]
+    pos, vel = A["pos"][a:b], A["vel"][a:b]
+    out = []
+    half = np.float32(0.5 * dx)
+    for d in range(3):
+        W, H, D = _face_dims(d, dims)
+        lo, hi = max(k0 - 2, 0), min(k1 + 2, D)
+        shifted = np.array(pos, np.float32, copy=True)
+        shifted[:, 2] -= np.float32(lo * dx)
+        off = np.array([half, half, half], np.float32)
+        off[d] = 0.0
+        f = np.zeros((hi - lo, H, W), np.float32)
+        w = np.zeros_like(f)
+        vals = np.ascontiguousarray(vel[:, d])
+        O.lib().gfo_splat_add(shifted, vals, len(shifted), float(dx), off, float(dx), W, H, hi - lo, f, w)
+        out.append((lo, f, w))
+    return out
+
+
+def _g2p_range(task):
+    """PIC/FLIP update, RK4 advection and solid collisions of particles [a, b)."""
+    a, b, dims, dx, dt, ratio = task
+    O, A = _WORKER["O"], _WORKER["arr"]
+    pos, vel = A["pos"][a:b], A["vel"][a:b]
+    new = (A["u"], A["v"], A["w"])
+    old = (A["su"], A["sv"], A["sw"])
+    A["vel_out"][a:b] = O.flip_update(dims, dx, ratio, new, old, pos, vel)
+    p1 = O.advect_rk4(dims, dx, *new, dt, pos)
+    A["pos_out"][a:b] = O.resolve_collisions(dims, dx, A["mat"], pos, p1)
+    return b - a
+
+
+def cpu_substep(sc, workers):
+    """One measured CPU substep of scene `sc`; returns (seconds, stage seconds,
+    CG iterations, particles, worker count)."""
+    import multiprocessing as mp
+    from multiprocessing import shared_memory
+    import oracle as O
+    dims, dx, dt = sc.dims, sc.dx, sc.dt
+    ni, nj, nk = dims
+    g = np.array(sc.gravity, np.float32)
+    shms = []
+
+    def shared(shape, dtype):
+        a = np.zeros(shape, dtype)
+        sh = shared_memory.SharedMemory(create=True, size=max(a.nbytes, 1))
+        shms.append(sh)
+        return np.ndarray(shape, dtype=dtype, buffer=sh.buf), sh.name
+
+    st = {}
+    try:
+        mat = sc.mat.copy()
+        pos, vel, ids = sc.pos.copy(), sc.vel.copy(), sc.ids.copy()
+        t0 = time.perf_counter()
+        n = O.lib().gfo_update_fluid_cells(*dims, dx, mat, pos, vel, ids, len(pos))
+        st["update_fluid_cells"] = time.perf_counter() - t0
+        spec = {}
+        arrs = {}
+        for key, shape, dtype in (("pos", (n, 3), np.float32), ("vel", (n, 3), np.float32),
+                                  ("pos_out", (n, 3), np.float32), ("vel_out", (n, 3), np.float32),
+                                  ("mat", mat.shape, np.uint8),
+                                  ("u", (nk, nj, ni + 1), np.float32), ("v", (nk, nj + 1, ni), np.float32),
+                                  ("w", (nk + 1, nj, ni), np.float32), ("su", (nk, nj, ni + 1), np.float32),
+                                  ("sv", (nk, nj + 1, ni), np.float32), ("sw", (nk + 1, nj, ni), np.float32)):
+            arrs[key], nm = shared(shape, dtype)
+            spec[key] = (nm, shape, np.dtype(dtype).str)
+        arrs["pos"][:] = pos[:n]
+        arrs["vel"][:] = vel[:n]
+        arrs["mat"][:] = mat
+        del pos, vel
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(workers, initializer=_worker_init, initargs=(spec,)) as pool:
+            pool.map(_g2p_range, [(0, 0, dims, dx, dt, 0.05)])   # workers up before timing
+            # stage 5: velocity splat over k-slabs of the cell-ordered particles
+            t0 = time.perf_counter()
+            cellk = np.floor(arrs["pos"][:, 2].astype(np.float64) / dx).astype(np.int64)
+            bounds = np.searchsorted(cellk, np.linspace(0, nk, 4 * workers + 1).round().astype(np.int64))
+            ks = np.linspace(0, nk, 4 * workers + 1).round().astype(int)
+            tasks = [(int(bounds[q]), int(bounds[q + 1]), int(ks[q]), int(ks[q + 1]), dims, dx)
+                     for q in range(4 * workers) if bounds[q + 1] > bounds[q]]
+            fields = [np.zeros(_face_dims(d, dims)[::-1], np.float32) for d in range(3)]
+            weights = [np.zeros_like(f) for f in fields]
+            for part in pool.imap_unordered(_splat_slab, tasks):
+                for d, (lo, f, w) in enumerate(part):
+                    fields[d][lo:lo + f.shape[0]] += f
+                    weights[d][lo:lo + f.shape[0]] += w
+            st["splat_particles"] = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            mac = [arrs["u"], arrs["v"], arrs["w"]]
+            for d in range(3):
+                O.lib().gfo_velocity_from_splat(d, ni, nj, nk, mat, fields[d], weights[d], mac[d])
+            st["splat_weight_and_fill"] = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            saved = O.extrapolate(dims, mat, 7, *mac)
+            for key, a in zip(("su", "sv", "sw"), saved):
+                arrs[key][:] = a
+            st["extrapolate_saved"] = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            u, v, w = O.body_force(dims, mat, g, dt, *mac)
+            st["body_force"] = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            p, iters, _ = O.pressure_solve(dims, dx, 20.0, dt, mat, u, v, w)
+            pg = O.pressure_to_grid(dims, mat, p)
+            st["pressure"] = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            u, v, w = O.apply_pressure(dims, dx, 20.0, dt, mat, pg, u, v, w)
+            st["apply_pressure"] = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            u, v, w = O.extrapolate(dims, mat, 7, u, v, w)
+            arrs["u"][:], arrs["v"][:], arrs["w"][:] = u, v, w
+            st["extrapolate"] = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            step = max(1, -(-n // (8 * workers)))
+            list(pool.imap_unordered(_g2p_range, [(a, min(a + step, n), dims, dx, dt, float(np.float32(0.05)))
+                                                   for a in range(0, n, step)]))
+            st["g2p_rk4_collisions"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        pos1, vel1 = arrs["pos_out"].copy(), arrs["vel_out"].copy()
+        O.lib().gfo_cap_particles_per_cell(*dims, dx, 100, pos1, vel1, ids[:n].copy(), n)
+        st["per_cell_cap"] = time.perf_counter() - t0
+    finally:
+        for sh in shms:
+            sh.close()
+            sh.unlink()
+    return sum(st.values()), st, iters, n, workers
+
+
 def reference_main(args):
     r, world, _ = rank_info()
     if r != 0:
         return 0
     sc = make_scene()
-    iters = args.ref_cg_iterations
-    times = []
-    wall = 0.0
-    for s in range(args.warmup + args.steps):
-        tot, parts, w, ns, n = cpu_estimate(sc, iters, seed=s)
-        wall += w
-        if s >= args.warmup:
-            times.append(tot)
-    t = statistics.mean(times)
+    workers = max(1, min(os.cpu_count() or 1, 64))
+    t_run = time.perf_counter()
+    t, parts, iters, n, workers = cpu_substep(sc, workers)
+    t_run = time.perf_counter() - t_run
     value = 1.0 / t
-    sample = (f"per step: oracle single-thread, all grid-wide stages of the 256^3 scene at full size, "
-              f"particle stages on {ns} of {n} particles scaled x{n / ns:.1f}, pressure set-up + "
-              f"per-iteration cost scaled to {iters} CG iterations (PLAIN FP64, the reference's solver)")
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+    sample = (f"one whole substep of the workload, every stage on all {n} particles and the full 256^3 "
+              f"grids (nothing extrapolated): the oracle's stages timed one after another; the splat and "
+              f"the PIC/FLIP + RK4 + collision pass on {workers} processes, the grid stages and the FP64 "
+              f"MIC(0)-PCG ({iters} iterations, run to the reference's rule) on one core")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": 1,
+            "warmup": 0, "steps_requested": args.steps, "warmup_requested": args.warmup,
+            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 particles/grid, f64 PCG", "data": "synthetic (seeded)",
             "impl": "reference",
             "config": {"workload": "slab_spheres 256^3 dx=1/32, ~40M particles, 1 substep of 1/30 s",
-                       "particles": n, "parallelism": "none (single-threaded CPU)"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample,
+                       "particles": n, "parallelism": f"{workers} host processes for the particle stages"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port", "sample": sample,
+                             "cg_iterations": iters, "wall_s": round(t_run, 1),
                              "stage_seconds": {k: round(v, 4) for k, v in parts.items()}},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -426,6 +594,99 @@ def next_rows_bench(ctx, sim, sample=200_000, seed=0):
                           "gpu_mpoints_s": round(len(pts) / t_gpu / 1e6, 1), "cpu_s_estimate": round(t_cpu, 1),
                           "cpu_sample": f"oracle single thread on {sample} points, scaled"}
     out["note"] = "wall clock around each drop-in call, host arrays in and out"
+    return out
+
+
+def oracle_check(sim, sc, warmup, sample=400_000, seed=0):
+    """Untimed parity of one substep of the 256^3 workload against the oracle,
+    after `warmup` substeps:
+
+    pressure_plain   the PLAIN solve of the substep's system (the device's own
+                     field after the body force) against the oracle's FP64 PCG
+                     of the same system: CG iterations (+-1 is the bar) and
+                     max|p - p_ref| / max|p_ref| of the float pressure grids;
+    pressure_mixed   the MIXED solve against the oracle solved to max|r| < 1e-10;
+    positions        the substep's PIC/FLIP + RK4 + collision pass on a sample of
+                     particles, recomputed by the oracle from the device's own
+                     grids (the field after extrapolation and the saved field):
+                     max position error in cells (1e-5 is the bar) and max
+                     velocity error relative to the sample's velocity scale."""
+    import oracle as O
+    from gridfluidsim3d_gb300 import PRECISION_MIXED, PRECISION_PLAIN, STAGE_BODY_FORCES, STAGE_PRESSURE
+    dims, dx, dt = sc.dims, sc.dx, sc.dt
+    out = {}
+    sim.precision = PRECISION_PLAIN
+    reset(sim, sc)
+    run_steps(sim, sc, warmup, dt)
+    sim.step_stages(dt, STAGE_BODY_FORCES)
+    f = sim.get_velocity_field()
+    mat = sim.get_material_grid()
+    t0 = time.perf_counter()
+    p_ref, it_ref, _ = O.pressure_solve(dims, dx, 20.0, dt, mat, f.u, f.v, f.w)
+    t_plain = time.perf_counter() - t0
+    g_ref = O.pressure_to_grid(dims, mat, p_ref)
+    st = sim.step_stages(dt, STAGE_PRESSURE)
+    g = sim.get_pressure_grid()
+    scale = float(np.abs(g_ref).max())
+    out["pressure_plain"] = {"cg_iterations": st["cg_iterations"], "oracle_cg_iterations": it_ref,
+                             "rel_error": float(np.abs(g - g_ref).max() / scale), "oracle_s": round(t_plain, 1)}
+    t0 = time.perf_counter()
+    # the FP64 reference solution: max|r| < 1e-10 absolute, about 3e-12 of max|b| here
+    p_x, it_x, _ = O.pressure_solve(dims, dx, 20.0, dt, mat, f.u, f.v, f.w, tol=1e-10, max_iters=1000)
+    t_exact = time.perf_counter() - t0
+    g_x = O.pressure_to_grid(dims, mat, p_x)
+    sim.precision = PRECISION_MIXED
+    st = sim.step_stages(dt, STAGE_PRESSURE)
+    g = sim.get_pressure_grid()
+    out["pressure_mixed"] = {"inner_iterations": st["cg_iterations"], "fp64_residual": st["cg_max_residual"],
+                             "rel_error_vs_oracle_fp64": float(np.abs(g - g_x).max() / np.abs(g_x).max()),
+                             "oracle_iterations_to_1e-10": it_x, "oracle_s": round(t_exact, 1)}
+    # one whole mixed substep, then the oracle's G2P on the device's grids
+    pos0, vel0, ids0 = sim.get_marker_particles()
+    sim.update(dt)
+    fn, fs = sim.get_velocity_field(), sim.get_saved_velocity_field()
+    mat = sim.get_material_grid()
+    pos1, vel1, ids1 = sim.get_marker_particles()
+    rng = np.random.default_rng(seed)
+    sel = np.sort(rng.choice(len(ids0), size=min(sample, len(ids0)), replace=False))
+    sp, sv, sid = pos0[sel], vel0[sel], ids0[sel]
+    v_ref = O.flip_update(dims, dx, float(np.float32(0.05)), (fn.u, fn.v, fn.w), (fs.u, fs.v, fs.w), sp, sv)
+    p_ref = O.resolve_collisions(dims, dx, mat, sp, O.advect_rk4(dims, dx, fn.u, fn.v, fn.w, dt, sp))
+    where = np.full(int(max(ids1.max(), ids0.max())) + 1, -1, np.int64)
+    where[ids1] = np.arange(len(ids1))
+    q = where[sid]
+    kept = q >= 0
+    err = float(np.abs(pos1[q[kept]] - p_ref[kept]).max() / dx)
+    vscale = max(float(np.abs(v_ref).max()), 1e-3)
+    out["positions"] = {"sample": int(kept.sum()), "max_error_cells": err,
+                        "max_velocity_error_rel": float(np.abs(vel1[q[kept]] - v_ref[kept]).max() / vscale)}
+    return out
+
+
+def configs_bench(ctx, warmup=3):
+    """The two other forward configurations, timed on the device (CUDA events on
+    the library stream around the whole run): the 64^3 ball drop over its 30
+    substeps (one per 1/30 s frame), and the 128^3 dam break over 60 substeps,
+    each in both pressure forms from the same initial state."""
+    import torch
+    from gridfluidsim3d_gb300 import PRECISION_MIXED, PRECISION_PLAIN, FluidSimulation, scenes
+    out = {}
+    for name, sc, steps in (("ball_drop_64", scenes.ball_drop(64), 30), ("dam_break_128", scenes.dam_break(128), 60)):
+        res = {"particles": sc.num_particles, "substeps": steps}
+        for form, prec in (("plain", PRECISION_PLAIN), ("mixed", PRECISION_MIXED)):
+            sim = FluidSimulation(*sc.dims, sc.dx, max_particles=sc.num_particles, ctx=ctx)
+            sim.precision = prec
+            for rep in range(2):           # the first run warms up (module load, allocation)
+                reset(sim, sc)
+                t, stats, launches = timed(ctx, sim, sc, steps if rep else warmup, sc.dt, lambda: None)
+            res[form] = {"substeps_per_s": steps / t, "ms_total": round(t * 1e3, 2),
+                         "cg_iterations": [s["cg_iterations"] for s in stats],
+                         "max_residual": max(s["cg_max_residual"] for s in stats),
+                         "particles_end": stats[-1]["num_particles"], "gpu_launches": int(launches)}
+            sim.close()
+        res["mixed_over_plain"] = res["mixed"]["substeps_per_s"] / res["plain"]["substeps_per_s"]
+        out[name] = res
+    torch.cuda.synchronize()
     return out
 
 
@@ -604,6 +865,11 @@ def main(args):
     ctx.synchronize()
     te = reduce_max(time.perf_counter() - t0, world)
 
+    check = configs = None
+    if r == 0 and world == 1 and not args.no_check and set(forms) == {"plain", "mixed"}:
+        check = oracle_check(sim, sc, args.warmup)
+    if r == 0 and world == 1 and not args.no_configs and set(forms) == {"plain", "mixed"}:
+        configs = configs_bench(ctx)
     savestate = sources = next_rows = None
     if r == 0 and world == 1 and not args.no_savestate and set(forms) == {"plain", "mixed"}:
         savestate = savestate_bench(sim)
@@ -677,6 +943,8 @@ def main(args):
                       "max_residual": [s["cg_max_residual"] for s in plain["stats"]],
                       "ms_per_stage": pbreak},
             "accuracy_vs_fp64": accuracy,
+            "oracle_check": check,
+            "configs": configs,
             "mixed": {"cg_iterations": [s["cg_iterations"] for s in st],
                       "refinements": [s["refinements"] for s in st],
                       "max_residual": [s["cg_max_residual"] for s in st],
@@ -713,8 +981,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-rollout leg")
     ap.add_argument("--no-check", action="store_true", help="skip the per-step FP64 pressure check")
     ap.add_argument("--no-savestate", action="store_true", help="skip the savestate write/read leg")
-    ap.add_argument("--ref-cg-iterations", type=int, default=200,
-                    help="CG iterations the reference arm scales its per-iteration cost to")
+    ap.add_argument("--no-configs", action="store_true", help="skip the 64^3 / 128^3 forward configurations")
     a = ap.parse_args()
     if a.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -102,6 +102,11 @@ _SIGNATURES = {
     "gfs_sim_set_material": [_P, _P],
     "gfs_sim_get_material": [_P, _P],
     "gfs_sim_set_particles": [_P, _P, _P, _P, _I64],
+    "gfs_sim_add_solid_cells": [_P, _P, _I],
+    "gfs_sim_remove_solid_cells": [_P, _P, _I],
+    "gfs_sim_initialize": [_P, _P, _I, _P, _I, ctypes.POINTER(_I64)],
+    "gfs_seed_fluid_particles": [_I, _I, _I, _D, _P, _P, _I, _P, _I, _D, ctypes.c_uint64, _P, _I64,
+                                 ctypes.POINTER(_I64)],
     "gfs_sim_num_particles": [_P, ctypes.POINTER(_I64)],
     "gfs_sim_get_particles": [_P, _P, _P, _P, ctypes.POINTER(_I64)],
     "gfs_sim_get_velocity_field": [_P, _P, _P, _P],
@@ -110,6 +115,7 @@ _SIGNATURES = {
     "gfs_sim_step_host": [_P, _D, _P, _P, _P, ctypes.POINTER(_I64), ctypes.POINTER(StepStats)],
     "gfs_sim_step_stages": [_P, _D, _I, ctypes.POINTER(StepStats)],
     "gfs_sim_get_saved_velocity_field": [_P, _P, _P, _P],
+    "gfs_sim_add_marker_particle_points": [_P, _D, _P, _D, _I, _I, _I, _P, _I, _D],
     "gfs_sim_pressure_check": [_P, _D, _D, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_I)],
     "gfs_sim_set_fluid_sources": [_P, ctypes.POINTER(FluidSourceC), _I],
     "gfs_sim_set_marker_particle_jitter": [_P, _D, ctypes.c_uint64],

@@ -20,8 +20,10 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgfs.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code keeps the reference's float / double steps: no a*b+c contraction into FMA
+# (GCC contracts by default on aarch64), so both machines give identical bits
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-Wall", "-I" + INCLUDE, "-I" + CSRC]
+              "-Xcompiler", "-Wall", "-Xcompiler", "-ffp-contract=off", "-I" + INCLUDE, "-I" + CSRC]
 
 
 def nvcc() -> str:

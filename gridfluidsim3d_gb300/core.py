@@ -378,9 +378,13 @@ class FluidSimulation:
     not part of this core.
     """
 
-    def __init__(self, isize, jsize, ksize, dx, max_particles, ctx: Context | None = None):
+    def __init__(self, isize, jsize, ksize, dx, max_particles=None, ctx: Context | None = None):
+        """max_particles: the device capacity; None reserves 8 per cell, the most
+        initialize() can seed."""
         self.ctx = ctx or Context.default()
         self.isize, self.jsize, self.ksize, self.dx = int(isize), int(jsize), int(ksize), float(dx)
+        if max_particles is None:
+            max_particles = 8 * self.isize * self.jsize * self.ksize
         h = ctypes.c_void_p()
         _lib.lib().gfs_sim_create(self.ctx.handle, self.isize, self.jsize, self.ksize, self.dx, int(max_particles),
                                   ctypes.byref(h))
@@ -390,6 +394,69 @@ class FluidSimulation:
         self.last_stats = None
         self.current_frame = 0
         self._autosave = False
+        self._fluid_points = []     # FluidSimulation::_fluidPoints (fluidsimulation.h:1112)
+        self._fluid_cuboids = []    # FluidSimulation::_fluidCuboids
+        self._initialized = False
+
+    # -- scene set-up (fluidsimulation.cpp:48-55, 703-765, 845-885; pyfluid/fluidsimulation.py:89-101,
+    #    609-671) --
+    def add_implicit_fluid_point(self, x, y=None, z=None, radius=None):
+        """addImplicitFluidPoint(x, y, z, r) or (p, r): a sphere of fluid seeded by initialize()."""
+        if radius is None and z is None:
+            (x, y, z), radius = x, y
+        if not radius >= 0.0:
+            raise GFSError(_lib.GFS_ERR_INVALID, "add_implicit_fluid_point", "radius must be >= 0")
+        if self._initialized:
+            raise GFSError(_lib.GFS_ERR_STATE, "add_implicit_fluid_point", "the simulation is already initialized")
+        self._fluid_points.append((float(x), float(y), float(z), float(radius)))
+
+    def add_fluid_cuboid(self, *args):
+        """addFluidCuboid: an AABB (position, width, height, depth attributes, as
+        pyfluid's AABB), (x, y, z, w, h, d), (p, w, h, d) or two opposite corners."""
+        if len(args) == 1:
+            b = args[0]
+            p, w, h, d = b.position, b.width, b.height, b.depth
+        elif len(args) == 2:
+            p1, p2 = (tuple(float(c) for c in a) for a in args)
+            p = tuple(min(a, b) for a, b in zip(p1, p2))
+            w, h, d = (abs(b - a) for a, b in zip(p1, p2))
+        elif len(args) == 4:
+            p, w, h, d = args
+        elif len(args) == 6:
+            p, (w, h, d) = args[:3], args[3:]
+        else:
+            raise TypeError("add_fluid_cuboid takes an AABB, two corners, (p, w, h, d) or (x, y, z, w, h, d)")
+        if not (w >= 0 and h >= 0 and d >= 0):
+            raise GFSError(_lib.GFS_ERR_INVALID, "add_fluid_cuboid", "dimensions must be >= 0")
+        if self._initialized:
+            raise GFSError(_lib.GFS_ERR_STATE, "add_fluid_cuboid", "the simulation is already initialized")
+        self._fluid_cuboids.append(tuple(float(c) for c in p) + (float(w), float(h), float(d)))
+
+    def add_solid_cells(self, cell_list):
+        """addSolidCells: cells (GridIndex objects or (i, j, k) rows) become solid."""
+        c = self._cells(cell_list)
+        _lib.lib().gfs_sim_add_solid_cells(self._h, _p(c), len(c))
+
+    def remove_solid_cells(self, cell_list):
+        """removeSolidCells: solid cells of the list become air."""
+        c = self._cells(cell_list)
+        _lib.lib().gfs_sim_remove_solid_cells(self._h, _p(c), len(c))
+
+    def initialize(self):
+        """FluidSimulation::initialize: solid border, then the fluid seeded from the
+        implicit points and cuboids (8 particles per full cell on the 2x2x2
+        sub-lattice, sub-cell particles at the surface), with the jitter of
+        set_marker_particle_jitter (factor 0.1 by default)."""
+        if self._initialized:
+            return
+        pts = np.ascontiguousarray(np.array(self._fluid_points, np.float64).reshape(-1, 4))
+        cub = np.ascontiguousarray(np.array(self._fluid_cuboids, np.float64).reshape(-1, 6))
+        n = ctypes.c_int64(0)
+        _lib.lib().gfs_sim_initialize(self._h, _p(pts), len(pts), _p(cub), len(cub), ctypes.byref(n))
+        self._initialized = True
+
+    def is_initialized(self) -> bool:
+        return self._initialized
 
     # -- parameters (fluidsimulation.h:146-446 setters) --
     def _push(self):
@@ -491,6 +558,19 @@ class FluidSimulation:
         out = np.zeros((self.ksize, self.jsize, self.isize), np.float32)
         _lib.lib().gfs_sim_get_pressure_grid(self._h, _p(out))
         return out
+
+    def add_marker_particle_points(self, radius, offset, dx, field, threshold=None):
+        """CLScalarField::addPoints of the simulation's device-resident marker
+        particles (the scalar field IsotropicParticleMesher builds every substep):
+        field (3-D float32, shape (D, H, W)) += the splat of every particle.  The
+        positions never leave the device."""
+        if field.dtype != np.float32 or not field.flags.c_contiguous or field.ndim != 3:
+            raise GFSError(_lib.GFS_ERR_INVALID, "add_marker_particle_points",
+                           "field must be a contiguous 3-D float32 array")
+        D, H, W = field.shape
+        off = _arr(offset, np.float32)
+        _lib.lib().gfs_sim_add_marker_particle_points(self._h, float(radius), _p(off), float(dx), W, H, D, _p(field),
+                                                      int(threshold is not None), float(threshold or 0.0))
 
     def get_saved_velocity_field(self) -> MACVelocityField:
         """The last step's saved field (after _advectVelocityField, extrapolated),

@@ -263,6 +263,7 @@ static int sim_set_particles(Sim *s, const float *hp, const float *hv, const uin
     GFS_CUDA_CHECK(cudaMemcpyAsync(s->num.p, &hn, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     s->n_bound = n;
     s->need_sort = true;
+    s->sorted_hint = true;   // e.g. the set a step handed back: the sort keeps it in place
     // particles that fluid sources add take ids after every id given so far; with
     // caller ids the maximum is found on the device when a source first needs it
     s->next_id = (uint32_t)n;
@@ -656,6 +657,83 @@ int gfs_sim_get_material(gfs_sim *sim, uint8_t *h_material) {
     return download_padded<uint8_t>(sim->s.ctx, sim->s.mat.as<uint8_t>(), sim->s.g.c, h_material, stage);
 }
 
+static int set_solid_cells(gfs_sim *sim, const int32_t *ijk, int n, bool solid) {
+    GFS_NONNULL(sim);
+    Sim *s = &sim->s;
+    if (n < 0 || (n > 0 && !ijk)) {
+        set_error(GFS_ERR_INVALID, "solid cell list: invalid arguments");
+        return GFS_ERR_INVALID;
+    }
+    const int ni = s->g.ni, nj = s->g.nj, nk = s->g.nk;
+    for (int q = 0; q < n; q++) {
+        const int32_t *c = ijk + 3 * q;
+        if (c[0] < 0 || c[1] < 0 || c[2] < 0 || c[0] >= ni || c[1] >= nj || c[2] >= nk) {
+            set_error(GFS_ERR_INVALID, "solid cell index out of range: i: %d j: %d k: %d", c[0], c[1], c[2]);
+            return GFS_ERR_INVALID;
+        }
+    }
+    if (n == 0) return GFS_OK;
+    std::vector<uint8_t> mat((size_t)ni * nj * nk);
+    DevMem stage;
+    int rc = download_padded<uint8_t>(s->ctx, s->mat.as<uint8_t>(), s->g.c, mat.data(), stage);
+    if (rc) return rc;
+    for (int q = 0; q < n; q++) {
+        const int32_t *c = ijk + 3 * q;
+        uint8_t &m = mat[(size_t)c[0] + (size_t)ni * ((size_t)c[1] + (size_t)nj * c[2])];
+        if (solid) m = GFS_SOLID;
+        else if (m == GFS_SOLID) m = GFS_AIR;
+    }
+    rc = upload_padded<uint8_t>(s->ctx, mat.data(), s->g.c, s->mat.as<uint8_t>(), stage);
+    if (rc) return rc;
+    GFS_CUDA_CHECK(cudaStreamSynchronize(s->ctx->stream));
+    s->need_sort = true;   // particles in new solid cells go at the next step
+    return GFS_OK;
+}
+
+int gfs_sim_add_solid_cells(gfs_sim *sim, const int32_t *ijk, int n) { return set_solid_cells(sim, ijk, n, true); }
+
+int gfs_sim_remove_solid_cells(gfs_sim *sim, const int32_t *ijk, int n) { return set_solid_cells(sim, ijk, n, false); }
+
+int gfs_sim_initialize(gfs_sim *sim, const double *points, int npoints, const double *cuboids, int ncuboids,
+                       int64_t *num_particles) {
+    GFS_NONNULL(sim);
+    Sim *s = &sim->s;
+    if (npoints < 0 || ncuboids < 0 || (npoints > 0 && !points) || (ncuboids > 0 && !cuboids)) {
+        set_error(GFS_ERR_INVALID, "gfs_sim_initialize: invalid arguments");
+        return GFS_ERR_INVALID;
+    }
+    const int ni = s->g.ni, nj = s->g.nj, nk = s->g.nk;
+    if (ni < 3 || nj < 3 || nk < 3) {
+        set_error(GFS_ERR_INVALID, "gfs_sim_initialize: the grid needs at least 3 cells per axis");
+        return GFS_ERR_INVALID;
+    }
+    std::vector<uint8_t> mat((size_t)ni * nj * nk);
+    DevMem stage;
+    int rc = download_padded<uint8_t>(s->ctx, s->mat.as<uint8_t>(), s->g.c, mat.data(), stage);
+    if (rc) return rc;
+    std::vector<float> pos;
+    std::vector<uint8_t> mat_out;
+    rc = seed_fluid_particles(ni, nj, nk, s->g.dx, mat.data(), points, npoints, cuboids, ncuboids, s->jitter_factor,
+                              s->jitter_seed, pos, &mat_out);
+    if (rc) return rc;
+    const int64_t n = (int64_t)(pos.size() / 3);
+    if (n > s->capacity) {
+        set_error(GFS_ERR_INVALID, "gfs_sim_initialize: the fluid needs %lld particles, the simulation holds %lld",
+                  (long long)n, (long long)s->capacity);
+        return GFS_ERR_INVALID;
+    }
+    rc = upload_padded<uint8_t>(s->ctx, mat_out.data(), s->g.c, s->mat.as<uint8_t>(), stage);
+    if (rc) return rc;
+    std::vector<float> vel(pos.size(), 0.0f);
+    rc = sim_set_particles(s, pos.data(), vel.data(), nullptr, n);
+    if (rc) return rc;
+    if ((rc = sort_particles(s, true))) return rc;
+    if ((rc = classify_cells(s))) return rc;
+    GFS_CUDA_CHECK(cudaStreamSynchronize(s->ctx->stream));
+    if (num_particles) *num_particles = n;
+    return GFS_OK;
+}
+
 int gfs_sim_set_particles(gfs_sim *sim, const float *h_positions, const float *h_velocities,
                           const uint32_t *h_ids, int64_t n) {
     GFS_NONNULL(sim);
@@ -952,6 +1030,35 @@ int gfs_diff_info(gfs_diff *d, double *forward_ms, double *backward_ms, int64_t 
     long long b = 0;
     diff_info(d->d, forward_ms, backward_ms, &b);
     if (device_bytes) *device_bytes = b;
+    return GFS_OK;
+}
+
+int gfs_sim_add_marker_particle_points(gfs_sim *sim, double radius, const float offset[3], double dx, int W,
+                                       int H, int D, float *h_field, int threshold_set, double threshold) {
+    GFS_NONNULL(sim);
+    GFS_NONNULL(offset);
+    GFS_NONNULL(h_field);
+    const long long nodes = (long long)W * H * D;
+    if (W <= 0 || H <= 0 || D <= 0 || nodes >= 0xFFFFFFFFll || !(dx > 0) || !(radius > 0) || !std::isfinite(radius)) {
+        set_error(GFS_ERR_INVALID, "invalid point splat arguments (W=%d H=%d D=%d dx=%g radius=%g)", W, H, D, dx,
+                  radius);
+        return GFS_ERR_INVALID;
+    }
+    Sim *s = &sim->s;
+    Ctx *c = s->ctx;
+    int64_t n = 0;
+    int rc = sim_stage_xyz(s, &n);   // the resident particles as xyz triples, in the simulation's scratch
+    if (rc) return rc;
+    if (n == 0) return GFS_OK;
+    DevMem df;
+    const size_t fbytes = (size_t)nodes * sizeof(float);
+    if (df.alloc(fbytes)) return GFS_ERR_NOMEM;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(df.p, h_field, fbytes, cudaMemcpyHostToDevice, c->stream));
+    rc = splat_points(c, s->pos_alt.as<float>(), nullptr, n, radius, offset, dx, W, H, D, df.as<float>(), nullptr,
+                      threshold_set != 0, (float)threshold);
+    if (rc) return rc;
+    GFS_CUDA_CHECK(cudaMemcpyAsync(h_field, df.p, fbytes, cudaMemcpyDeviceToHost, c->stream));
+    GFS_CUDA_CHECK(cudaStreamSynchronize(c->stream));
     return GFS_OK;
 }
 

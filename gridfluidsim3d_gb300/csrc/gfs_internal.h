@@ -122,6 +122,7 @@ struct Sim {
     int64_t capacity = 0;
     int64_t n_bound = 0;         // host-side upper bound of the particle count
     bool need_sort = false;      // particles not yet in (cell, id) order
+    bool sorted_hint = false;    // uploaded set may already be in order: the next sort checks first
     bool dx_pow2 = false;
     float inv_dx_f = 0.f;
     float bound_f[3] = {0, 0, 0}; // smallest floats >= dx*n (exact in-grid test)
@@ -170,6 +171,12 @@ int face_fill(Sim *s, double dt);     // a3 + saved copy + body forces
 int sim_step(Sim *s, double dt, gfs_step_stats *stats, int last_stage = GFS_STAGE_ALL);
 int sim_stage_xyz(Sim *s, int64_t *n_out);   // particles -> xyz triples in pos_alt / vel_alt (ids in key)
 int sim_unstage_xyz(Sim *s, int64_t n);      // n staged triples (ids 0..n-1) -> particles, sorted
+
+// ---- seeding.cu: FluidSimulation::_initializeFluidMaterial on the host (points: x y z r,
+// cuboids: x y z w h d); the material gets the solid border; out: xyz triples
+int seed_fluid_particles(int ni, int nj, int nk, double dx, const uint8_t *mat_in, const double *points,
+                         int npoints, const double *cuboids, int ncuboids, double jitter_factor,
+                         unsigned long long seed, std::vector<float> &out, std::vector<uint8_t> *mat_out);
 
 // ---- sources.cu
 int update_fluid_sources(Sim *s, int64_t *added, int64_t *removed);   // _updateFluidSources

@@ -230,43 +230,26 @@ int exclusive_scan_u32(Ctx *ctx, uint32_t *in, uint32_t *out, long long n, uint3
 
 // --------------------------------------------------------------- driver
 
-int sort_particles(Sim *s, bool /*remove_solid*/) {
+// The cap check of k_cell_sort for a set that was already in order: num[0] = the
+// particle count after removal, num[1] set if a cell holds more than `cap`.
+__global__ void k_cap_flag(const uint32_t *__restrict__ offset, long long ncells, int cap,
+                           uint32_t *__restrict__ num) {
+    long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    if (c == ncells - 1) num[0] = offset[ncells];
+    if ((int)(offset[c + 1] - offset[c]) > cap) atomicOr(&num[1], 1u);
+}
+
+// After the particles are in (cell, id) order: read the count and the cap flag;
+// cells holding more than max_particles_per_cell keep their smallest ids.
+static int finish_sort(Sim *s, long long ncells, bool /*was_in_order*/) {
     Ctx *ctx = s->ctx;
-    ProfScope prof(ctx, KC_SORT);
     cudaStream_t st = ctx->stream;
-    const GridDim &c = s->g.c;
-    long long ncells = (long long)c.nx * c.ny * c.nz;
-    long long nb = s->n_bound;
+    const int T = 256;
     uint32_t *count = s->count.as<uint32_t>();
     uint32_t *offset = s->offset.as<uint32_t>();
     uint32_t *num = s->num.as<uint32_t>();
-    GFS_CUDA_CHECK(cudaMemsetAsync(count, 0, (size_t)(ncells + 1) * sizeof(uint32_t), st));
-    GFS_CUDA_CHECK(cudaMemsetAsync(num + 1, 0, sizeof(uint32_t), st));
-    const int T = 256;
-    if (nb > 0) {
-        k_keys<<<grid_blocks(nb, T), T, 0, st>>>(s->pos.as<float4>(), num, nb, c, 1.0 / s->g.dx,
-                                                 s->inv_dx_f, s->dx_pow2 ? 1 : 0, s->mat.as<uint8_t>(),
-                                                 s->key.as<uint32_t>(), s->slot.as<uint32_t>(), count);
-        ctx->launches++;
-        GFS_LAUNCH_CHECK();
-    }
-    int rc = exclusive_scan_u32(ctx, count, offset, ncells + 1, s->scan_tmp.as<uint32_t>(), st);
-    if (rc) return rc;
-    if (nb > 0) {
-        k_scatter<<<grid_blocks(nb, T), T, 0, st>>>(s->pos.as<float4>(), s->vel.as<float4>(),
-                                                    s->key.as<uint32_t>(), s->slot.as<uint32_t>(),
-                                                    offset, num, nb, s->pos_alt.as<float4>(),
-                                                    s->vel_alt.as<float4>());
-        ctx->launches++;
-        GFS_LAUNCH_CHECK();
-    }
-    std::swap(s->pos.p, s->pos_alt.p);
-    std::swap(s->vel.p, s->vel_alt.p);
     int cap = s->params.max_particles_per_cell > 0 ? s->params.max_particles_per_cell : 0x7fffffff;
-    k_cell_sort<<<grid_blocks(ncells, T), T, 0, st>>>(s->pos.as<float4>(), s->vel.as<float4>(),
-                                                      offset, ncells, cap, num);
-    ctx->launches++;
-    GFS_LAUNCH_CHECK();
     uint32_t host_num[2];
     GFS_CUDA_CHECK(cudaMemcpyAsync(host_num, num, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     GFS_CUDA_CHECK(cudaStreamSynchronize(st));
@@ -275,7 +258,7 @@ int sort_particles(Sim *s, bool /*remove_solid*/) {
         k_cap_counts<<<grid_blocks(ncells + 1, T), T, 0, st>>>(offset, ncells, cap, count);
         ctx->launches++;
         GFS_LAUNCH_CHECK();
-        rc = exclusive_scan_u32(ctx, count, count, ncells + 1, s->scan_tmp.as<uint32_t>(), st);
+        int rc = exclusive_scan_u32(ctx, count, count, ncells + 1, s->scan_tmp.as<uint32_t>(), st);
         if (rc) return rc;
         k_cap_copy<<<grid_blocks(ncells, T), T, 0, st>>>(s->pos.as<float4>(), s->vel.as<float4>(),
                                                          offset, count, ncells, s->pos_alt.as<float4>(),
@@ -291,6 +274,86 @@ int sort_particles(Sim *s, bool /*remove_solid*/) {
     s->n_bound = host_num[0];
     s->need_sort = false;
     return GFS_OK;
+}
+
+// num[3] = 1 unless particles [0, n) are already in (cell, id) order with every
+// particle in a cell that keeps particles (keys from k_keys; ids in pos.w)
+__global__ void k_check_sorted(const float4 *__restrict__ pos, const uint32_t *__restrict__ key,
+                               const uint32_t *__restrict__ num, long long nbound, uint32_t *__restrict__ flag) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long n = nbound < (long long)num[0] ? nbound : (long long)num[0];
+    if (p >= n) return;
+    const uint32_t k1 = key[p];
+    bool bad = k1 == KEY_INVALID;
+    if (!bad && p > 0) {
+        const uint32_t k0 = key[p - 1];
+        bad = k0 > k1 || (k0 == k1 && pid(pos[p - 1]) >= pid(pos[p]));
+    }
+    if (bad) *flag = 1u;
+}
+
+int sort_particles(Sim *s, bool /*remove_solid*/) {
+    Ctx *ctx = s->ctx;
+    ProfScope prof(ctx, KC_SORT);
+    cudaStream_t st = ctx->stream;
+    const GridDim &c = s->g.c;
+    long long ncells = (long long)c.nx * c.ny * c.nz;
+    long long nb = s->n_bound;
+    uint32_t *count = s->count.as<uint32_t>();
+    uint32_t *offset = s->offset.as<uint32_t>();
+    uint32_t *num = s->num.as<uint32_t>();
+    GFS_CUDA_CHECK(cudaMemsetAsync(count, 0, (size_t)(ncells + 1) * sizeof(uint32_t), st));
+    GFS_CUDA_CHECK(cudaMemsetAsync(num + 1, 0, sizeof(uint32_t), st));
+    GFS_CUDA_CHECK(cudaMemsetAsync(num + 3, 0, sizeof(uint32_t), st));
+    const int T = 256;
+    if (nb > 0) {
+        k_keys<<<grid_blocks(nb, T), T, 0, st>>>(s->pos.as<float4>(), num, nb, c, 1.0 / s->g.dx,
+                                                 s->inv_dx_f, s->dx_pow2 ? 1 : 0, s->mat.as<uint8_t>(),
+                                                 s->key.as<uint32_t>(), s->slot.as<uint32_t>(), count);
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+    }
+    int rc = exclusive_scan_u32(ctx, count, offset, ncells + 1, s->scan_tmp.as<uint32_t>(), st);
+    if (rc) return rc;
+    // A set that is already in (cell, id) order with no particle to remove -- an
+    // upload of the particles a step handed back, or a load of a saved state --
+    // keeps its place: the offsets are all the sort has to produce.  The cap is
+    // then checked the way k_cell_sort checks it.
+    bool in_order = false;
+    if (s->sorted_hint && nb > 0) {
+        k_check_sorted<<<grid_blocks(nb, T), T, 0, st>>>(s->pos.as<float4>(), s->key.as<uint32_t>(), num, nb,
+                                                         num + 3);
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+        uint32_t host_flag = 1;
+        GFS_CUDA_CHECK(cudaMemcpyAsync(&host_flag, num + 3, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        GFS_CUDA_CHECK(cudaStreamSynchronize(st));
+        in_order = host_flag == 0;
+    }
+    s->sorted_hint = false;
+    if (in_order) {
+        int cap = s->params.max_particles_per_cell > 0 ? s->params.max_particles_per_cell : 0x7fffffff;
+        k_cap_flag<<<grid_blocks(ncells, T), T, 0, st>>>(offset, ncells, cap, num);
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+        return finish_sort(s, ncells, true);
+    }
+    if (nb > 0) {
+        k_scatter<<<grid_blocks(nb, T), T, 0, st>>>(s->pos.as<float4>(), s->vel.as<float4>(),
+                                                    s->key.as<uint32_t>(), s->slot.as<uint32_t>(),
+                                                    offset, num, nb, s->pos_alt.as<float4>(),
+                                                    s->vel_alt.as<float4>());
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+    }
+    std::swap(s->pos.p, s->pos_alt.p);
+    std::swap(s->vel.p, s->vel_alt.p);
+    int cap = s->params.max_particles_per_cell > 0 ? s->params.max_particles_per_cell : 0x7fffffff;
+    k_cell_sort<<<grid_blocks(ncells, T), T, 0, st>>>(s->pos.as<float4>(), s->vel.as<float4>(),
+                                                      offset, ncells, cap, num);
+    ctx->launches++;
+    GFS_LAUNCH_CHECK();
+    return finish_sort(s, ncells, false);
 }
 
 __global__ void k_classify(uint8_t *__restrict__ mat, GridDim c, const uint32_t *__restrict__ offset,

@@ -202,6 +202,43 @@ int gfs_sim_get_params(gfs_sim *sim, gfs_sim_params *p);
    (fluidsimulation.cpp:1933-1958). */
 int gfs_sim_set_material(gfs_sim *sim, const uint8_t *h_material);
 int gfs_sim_get_material(gfs_sim *sim, uint8_t *h_material);
+/* FluidSimulation::addSolidCells / removeSolidCells (fluidsimulation.cpp:845-885,
+   c_bindings/fluidsimulation_c.cpp FluidSimulation_add_solid_cells /
+   _remove_solid_cells): n cells (int32 triples i, j, k) become solid / a solid
+   cell becomes air.  An index out of range fails with GFS_ERR_INVALID and changes
+   nothing (the reference throws std::out_of_range).  Particles in new solid cells
+   are removed at the next step. */
+int gfs_sim_add_solid_cells(gfs_sim *sim, const int32_t *ijk, int n);
+int gfs_sim_remove_solid_cells(gfs_sim *sim, const int32_t *ijk, int n);
+
+/* FluidSimulation::initialize (fluidsimulation.cpp:48-55, 1407-1434) with the
+   implicit fluid points (addImplicitFluidPoint, :703-724; `points` holds npoints
+   rows x y z r) and fluid cuboids (addFluidCuboid, :726-765; `cuboids` holds
+   ncuboids rows x y z width height depth): the domain border becomes solid
+   (_initializeSolidCells) and the fluid is seeded from the scalar field of the
+   points and cuboids (_initializeFluidMaterial, :1383-1399; see
+   gfs_seed_fluid_particles): 8 particles on the 2x2x2 sub-lattice of every full
+   fluid cell, sub-cell particles inside the surface for the cells at the surface.
+   The particles replace the simulation's, at rest, ids 0..n-1; their jitter is
+   gfs_sim_set_marker_particle_jitter's (factor 0.1 by default; 0 reproduces the
+   reference's positions exactly).  *num_particles (may be NULL) receives the
+   count; more than the simulation's capacity fails with GFS_ERR_INVALID. */
+int gfs_sim_initialize(gfs_sim *sim, const double *points, int npoints, const double *cuboids, int ncuboids,
+                       int64_t *num_particles);
+
+/* The seeding of gfs_sim_initialize on the host alone (no device needed): the
+   marker-particle positions (xyz triples, in the reference's creation order: the
+   full cells' 8 particles cell by cell in k -> j -> i order, then the sub-cell
+   particles) of ni x nj x nk cells of width dx whose material is h_material (its
+   border is taken as solid).  h_positions = NULL queries the count into *n;
+   otherwise it must hold `capacity` >= *n triples.  jitter_factor in [0, 1]:
+   each component moves by a value in +-0.25 * jitter_factor * dx from a
+   counter-based hash of `seed` (the reference draws it from rand()). */
+int gfs_seed_fluid_particles(int ni, int nj, int nk, double dx, const uint8_t *h_material,
+                             const double *points, int npoints, const double *cuboids, int ncuboids,
+                             double jitter_factor, uint64_t seed, float *h_positions, int64_t capacity,
+                             int64_t *n);
+
 /* Replace the particle set (host -> device). ids may be NULL (0..n-1). */
 int gfs_sim_set_particles(gfs_sim *sim, const float *h_positions, const float *h_velocities,
                           const uint32_t *h_ids, int64_t n);
@@ -257,6 +294,18 @@ int gfs_sim_step_host(gfs_sim *sim, double dt, float *h_positions, float *h_velo
 #define GFS_STAGE_EXTRAPOLATE 9
 #define GFS_STAGE_ALL 12
 int gfs_sim_step_stages(gfs_sim *sim, double dt, int last_stage, gfs_step_stats *stats);
+/* CLScalarField::addPoints (clscalarfield.cpp:68-122, kernels/scalarfield.cl:
+   79-138) of the simulation's own marker particles, which never leave the
+   device: every particle adds w(|x - (p - offset)|^2 / radius^2) to each node x
+   of a W x H x D grid of spacing dx within `radius` (the splat of
+   gfs_scalar_field_add_point_values with every value 1), into h_field (host,
+   added to).  This is the scalar field IsotropicParticleMesher builds from the
+   marker positions inside every substep (isotropicparticlemesher.cpp:309-390);
+   the call replaces the host copy of 40M positions that the host-array entry
+   point needs.  threshold_set / threshold: as gfs_scalar_field_add_point_values. */
+int gfs_sim_add_marker_particle_points(gfs_sim *sim, double radius, const float offset[3], double dx, int W,
+                                       int H, int D, float *h_field, int threshold_set, double threshold);
+
 /* The saved field of the last (partial) step: the velocity field after
    _advectVelocityField, extrapolated (FluidSimulation::_savedVelocityField,
    fluidsimulation.cpp:3306-3307), which the PIC/FLIP update reads. */

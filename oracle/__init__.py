@@ -84,6 +84,7 @@ def lib():
         L.gfo_apply_weight.argtypes = [_i64, _f32p, _f32p]
         L.gfo_velocity_scalar_field.argtypes = [_i, _i, _i, _i, _d, _f32p, _f32p, _i64, _f32p, _u8p]
         L.gfo_advect_velocity_field.argtypes = [_i, _i, _i, _d, _u8p, _f32p, _f32p, _i64, _f32p, _f32p, _f32p]
+        L.gfo_velocity_from_splat.argtypes = [_i, _i, _i, _i, _u8p, _f32p, _f32p, _f32p]
         L.gfo_extrapolate.argtypes = [_i, _i, _i, _u8p, _i, _f32p, _f32p, _f32p]
         L.gfo_body_force.argtypes = [_i, _i, _i, _u8p, _f32p, _d, _f32p, _f32p, _f32p]
         L.gfo_pressure_solve.argtypes = [_i, _i, _i, _d, _d, _d, _u8p, _f32p, _f32p, _f32p, _d, _i,

@@ -166,6 +166,68 @@ void gfo_velocity_scalar_field(int dir, int ni, int nj, int nk, double dx,
 
 /* -------------------------------------------------- a3: face copy and fill */
 
+/* The face copy and 26-neighbour fill of one component (fluidsimulation.cpp:
+   2597-2736) from the splatted field `grid` (after applyWeightField) and its
+   is-set mask, into `out` (cleared first: _MACVelocity.clearU()). */
+void gfo_face_fill(int dir, int ni, int nj, int nk, const uint8_t *mat, const float *grid,
+                   const uint8_t *is_set, float *out) {
+    int W, H, D;
+    face_dims(dir, ni, nj, nk, &W, &H, &D);
+    int64_t count = (int64_t)W * H * D;
+    memset(out, 0, (size_t)count * sizeof(float));
+    /* extrapolationIndices: fluid-bordering faces without a value, in
+       k->j->i order (fluidsimulation.cpp:2604-2616) */
+    int64_t *queue = (int64_t *)malloc((size_t)count * sizeof(int64_t));
+    int64_t nq = 0;
+    for (int k = 0; k < D; k++)
+        for (int j = 0; j < H; j++)
+            for (int i = 0; i < W; i++) {
+                if (face_borders(mat, dir, i, j, k, ni, nj, nk, GFO_FLUID)) {
+                    int64_t f = idx3(i, j, k, W, H);
+                    if (!is_set[f]) queue[nq++] = f;
+                    else out[f] = grid[f];
+                }
+            }
+    /* 26-neighbour average (fluidsimulation.cpp:2618-2639); Grid3d::
+       getNeighbourGridIndices26 order is k, j, i ascending (grid3d.h:224-236).
+       U uses fabs(value) > 0, V and W use isValueSet (the reference's
+       asymmetry, :2630 vs :2675/:2720). */
+    for (int64_t q = 0; q < nq; q++) {
+        int64_t f = queue[q];
+        int gi = (int)(f % W), gj = (int)((f / W) % H), gk = (int)(f / ((int64_t)W * H));
+        double avg = 0.0, wsum = 0.0;
+        for (int kk = gk - 1; kk <= gk + 1; kk++)
+            for (int jj = gj - 1; jj <= gj + 1; jj++)
+                for (int ii = gi - 1; ii <= gi + 1; ii++) {
+                    if (ii == gi && jj == gj && kk == gk) continue;
+                    if (!in_range(ii, jj, kk, W, H, D)) continue;
+                    int64_t nf = idx3(ii, jj, kk, W, H);
+                    int ok = (dir == 0) ? (fabs((double)grid[nf]) > 0.0) : (is_set[nf] != 0);
+                    if (ok) {
+                        avg += (double)grid[nf];
+                        wsum += 1.0;
+                    }
+                }
+        if (wsum > 0.0) out[f] = (float)(avg / wsum);
+    }
+    free(queue);
+}
+
+/* _computeVelocityScalarField's tail (fluidsimulation.cpp:2567-2586) and the
+   fill, from a splat already accumulated into value / weight (value is divided
+   in place): the velocity component `dir` of _advectVelocityField. */
+void gfo_velocity_from_splat(int dir, int ni, int nj, int nk, const uint8_t *mat, float *value,
+                             const float *weight, float *out) {
+    int W, H, D;
+    face_dims(dir, ni, nj, nk, &W, &H, &D);
+    int64_t count = (int64_t)W * H * D;
+    uint8_t *is_set = (uint8_t *)malloc((size_t)count);
+    gfo_apply_weight(count, value, weight);
+    for (int64_t f = 0; f < count; f++) is_set[f] = ((double)weight[f] > 1e-9) ? 1 : 0;
+    gfo_face_fill(dir, ni, nj, nk, mat, value, is_set, out);
+    free(is_set);
+}
+
 void gfo_advect_velocity_field(int ni, int nj, int nk, double dx, const uint8_t *mat,
                                const float *pos, const float *vel, int64_t n,
                                float *u, float *v, float *w) {
@@ -176,46 +238,8 @@ void gfo_advect_velocity_field(int ni, int nj, int nk, double dx, const uint8_t 
         int64_t count = (int64_t)W * H * D;
         float *grid = (float *)malloc((size_t)count * sizeof(float));
         uint8_t *is_set = (uint8_t *)malloc((size_t)count);
-        float *out = mac[dir];
-        memset(out, 0, (size_t)count * sizeof(float)); /* _MACVelocity.clearU() */
         gfo_velocity_scalar_field(dir, ni, nj, nk, dx, pos, vel, n, grid, is_set);
-
-        /* extrapolationIndices: fluid-bordering faces without a value, in
-           k->j->i order (fluidsimulation.cpp:2604-2616) */
-        int64_t *queue = (int64_t *)malloc((size_t)count * sizeof(int64_t));
-        int64_t nq = 0;
-        for (int k = 0; k < D; k++)
-            for (int j = 0; j < H; j++)
-                for (int i = 0; i < W; i++) {
-                    if (face_borders(mat, dir, i, j, k, ni, nj, nk, GFO_FLUID)) {
-                        int64_t f = idx3(i, j, k, W, H);
-                        if (!is_set[f]) queue[nq++] = f;
-                        else out[f] = grid[f];
-                    }
-                }
-        /* 26-neighbour average (fluidsimulation.cpp:2618-2639); Grid3d::
-           getNeighbourGridIndices26 order is k, j, i ascending (grid3d.h:224-236).
-           U uses fabs(value) > 0, V and W use isValueSet (the reference's
-           asymmetry, :2630 vs :2675/:2720). */
-        for (int64_t q = 0; q < nq; q++) {
-            int64_t f = queue[q];
-            int gi = (int)(f % W), gj = (int)((f / W) % H), gk = (int)(f / ((int64_t)W * H));
-            double avg = 0.0, wsum = 0.0;
-            for (int kk = gk - 1; kk <= gk + 1; kk++)
-                for (int jj = gj - 1; jj <= gj + 1; jj++)
-                    for (int ii = gi - 1; ii <= gi + 1; ii++) {
-                        if (ii == gi && jj == gj && kk == gk) continue;
-                        if (!in_range(ii, jj, kk, W, H, D)) continue;
-                        int64_t nf = idx3(ii, jj, kk, W, H);
-                        int ok = (dir == 0) ? (fabs((double)grid[nf]) > 0.0) : (is_set[nf] != 0);
-                        if (ok) {
-                            avg += (double)grid[nf];
-                            wsum += 1.0;
-                        }
-                    }
-            if (wsum > 0.0) out[f] = (float)(avg / wsum);
-        }
-        free(queue);
+        gfo_face_fill(dir, ni, nj, nk, mat, grid, is_set, mac[dir]);
         free(grid);
         free(is_set);
     }

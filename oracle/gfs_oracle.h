@@ -65,6 +65,17 @@ void gfo_advect_velocity_field(int ni, int nj, int nk, double dx, const uint8_t 
                                const float *pos, const float *vel, int64_t n,
                                float *u, float *v, float *w);
 
+/* The copy into fluid-bordering faces and the 26-neighbour fill of one component
+   (out cleared first), from its splatted field and is-set mask. */
+void gfo_face_fill(int dir, int ni, int nj, int nk, const uint8_t *mat, const float *grid,
+                   const uint8_t *is_set, float *out);
+
+/* Component `dir` of _advectVelocityField from a splat already accumulated into
+   value / weight (gfo_splat_add, possibly in pieces): value /= weight, is-set
+   mask weight > 1e-9, then gfo_face_fill into out. */
+void gfo_velocity_from_splat(int dir, int ni, int nj, int nk, const uint8_t *mat, float *value,
+                             const float *weight, float *out);
+
 /* MACVelocityField::extrapolateVelocityField (macvelocityfield.cpp:754-797). */
 void gfo_extrapolate(int ni, int nj, int nk, const uint8_t *mat, int num_layers,
                      float *u, float *v, float *w);
