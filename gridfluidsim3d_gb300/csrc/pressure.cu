@@ -373,19 +373,25 @@ __device__ __forceinline__ T mic0_precon(unsigned nb, uint8_t fl, T pim1, T pjm1
 // whose tag equals the current epoch holds the producer's value for this sweep:
 // no progress counters and no memory fences are needed.  FP64 values travel as
 // two tagged words.
-// L2 load that the compiler keeps where it is written (polls and prefetches of
-// exchange words must not be merged, hoisted out of a loop or sunk to their use)
+// Exchange words are read and written with relaxed gpu-scope (strong) accesses.
+// A poll loop of weak loads may legally be collapsed into a single load by the
+// compiler (nothing in the loop orders it), after which it never sees the
+// producer's store; a strong load is performed on every iteration and must
+// eventually observe the strong store.  Both go to L2, like .cg accesses.
 __device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long *p) {
     unsigned long long v;
-    asm volatile("ld.global.cg.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 template <class T> struct Xch;
 template <> struct Xch<float> {
     static constexpr int W = 1;
     static __device__ __forceinline__ void put(unsigned long long *p, float v, unsigned tag) {
         unsigned long long w = ((unsigned long long)tag << 32) | (unsigned long long)__float_as_uint(v);
-        __stcg(p, w);
+        st_relaxed_u64(p, w);
     }
     static __device__ __forceinline__ void fetch(const unsigned long long *p, unsigned long long w[1]) {
         w[0] = ld_cg_u64(p);
@@ -401,8 +407,8 @@ template <> struct Xch<double> {
     static constexpr int W = 2;
     static __device__ __forceinline__ void put(unsigned long long *p, double v, unsigned tag) {
         unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-        __stcg(p, ((unsigned long long)tag << 32) | (bits & 0xFFFFFFFFull));
-        __stcg(p + 1, ((unsigned long long)tag << 32) | (bits >> 32));
+        st_relaxed_u64(p, ((unsigned long long)tag << 32) | (bits & 0xFFFFFFFFull));
+        st_relaxed_u64(p + 1, ((unsigned long long)tag << 32) | (bits >> 32));
     }
     static __device__ __forceinline__ void fetch(const unsigned long long *p, unsigned long long w[2]) {
         w[0] = ld_cg_u64(p);
