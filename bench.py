@@ -801,7 +801,8 @@ def main(args):
     _lib.load()
     sc = make_scene()
     ctx = Context(lr)
-    sim = FluidSimulation(*sc.dims, sc.dx, max_particles=sc.num_particles, ctx=ctx)
+    # room for the particles the fluid-source leg adds (an inflow sphere of radius 12 cells)
+    sim = FluidSimulation(*sc.dims, sc.dx, max_particles=sc.num_particles + 1_000_000, ctx=ctx)
     dt = sc.dt
     peak, peak_kind = load_peaks()
 

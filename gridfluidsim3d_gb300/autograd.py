@@ -40,6 +40,7 @@ class FlipRollout:
         h = ctypes.c_void_p()
         _lib.lib().gfs_diff_create(sim._h, self.nsteps, self.n, self.dt, ctypes.byref(h))
         self._h = h
+        sim._dependents.add(self)   # closed before the simulation it runs on
 
     def __call__(self, positions: torch.Tensor, u0=None, v0=None, w0=None, velocities=None):
         if velocities is None and (u0 is None or v0 is None or w0 is None):

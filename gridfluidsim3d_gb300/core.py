@@ -21,8 +21,10 @@ raises RuntimeError from its bindings.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes
 import os
+import weakref
 
 import numpy as np
 
@@ -87,8 +89,25 @@ class GridIndex:
         return f"GridIndex({self.i}, {self.j}, {self.k})"
 
 
+# Live contexts, closed at interpreter exit (each closes what was built on it first).
+_CONTEXTS = weakref.WeakSet()
+
+
+@atexit.register
+def _close_all():
+    for c in list(_CONTEXTS):
+        try:
+            c.close()
+        except Exception:
+            pass
+
+
 class Context:
-    """One CUDA device and stream (replaces the reference's OpenCL set-up)."""
+    """One CUDA device and stream (replaces the reference's OpenCL set-up).
+
+    A context outlives everything built on it: close() first closes the
+    simulations (and their rollouts) that use it, and every live context is
+    closed at interpreter exit in that order."""
 
     _default = None
 
@@ -98,6 +117,8 @@ class Context:
         L.gfs_ctx_create(device, ctypes.byref(h))
         self._h = h
         self.device = device
+        self._dependents = weakref.WeakSet()
+        _CONTEXTS.add(self)
 
     @classmethod
     def default(cls) -> "Context":
@@ -148,6 +169,8 @@ class Context:
         _lib.lib().gfs_ctx_inject_wait_timeout(self._h, int(sweeps))
 
     def close(self):
+        for d in list(getattr(self, "_dependents", ())):
+            d.close()
         if getattr(self, "_h", None) and self._h.value:
             _lib.lib().gfs_ctx_destroy(self._h)
             self._h = ctypes.c_void_p()
@@ -389,6 +412,8 @@ class FluidSimulation:
         _lib.lib().gfs_sim_create(self.ctx.handle, self.isize, self.jsize, self.ksize, self.dx, int(max_particles),
                                   ctypes.byref(h))
         self._h = h
+        self._dependents = weakref.WeakSet()   # rollouts built on this simulation
+        self.ctx._dependents.add(self)
         self._params = SimParams()
         _lib.lib().gfs_sim_default_params(ctypes.byref(self._params))
         self.last_stats = None
@@ -731,6 +756,8 @@ class FluidSimulation:
         return n.value, self.last_stats
 
     def close(self):
+        for d in list(getattr(self, "_dependents", ())):
+            d.close()
         if getattr(self, "_h", None) and self._h.value:
             _lib.lib().gfs_sim_destroy(self._h)
             self._h = ctypes.c_void_p()

@@ -16,7 +16,10 @@
 //      the checkpointed pressure, extrapolation);
 //   2. k_adj_g2p: per particle, the adjoint of the FLIP update and of RK4
 //      through the Jacobians of the Catmull-Rom samples; the sample adjoints
-//      scatter into the MAC / saved adjoint face grids (atomics);
+//      scatter into the MAC / saved adjoint face grids.  The scatter is in
+//      fixed point (64-bit integer atomics at a per-pass power-of-two scale
+//      found by a first pass over the particles), so the grids, and every
+//      gradient computed from them, are bitwise the same from run to run;
 //   3. k_adj_extrap_layer: adjoint of each extrapolation layer pass, in reverse
 //      layer order (a gather: a face receives from the layer faces it fed);
 //   4. pressure: p_bar = -k G^T u_bar on the fluid cells (k_adj_pbar), then
@@ -162,19 +165,60 @@ __device__ __forceinline__ float3 mtv(const float J[3][3], float3 c) {   // J^T 
 __device__ __forceinline__ float3 f3add(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
 __device__ __forceinline__ float3 f3scale(float3 a, float s) { return make_float3(a.x * s, a.y * s, a.z * s); }
 
-__global__ void __launch_bounds__(128) k_adj_g2p(AdvArgs A, const float4 *__restrict__ pos,
-                                                 const float4 *__restrict__ vel, long long n,
-                                                 const float *__restrict__ mu, const float *__restrict__ mv,
-                                                 const float *__restrict__ mw, const float *__restrict__ su,
-                                                 const float *__restrict__ sv, const float *__restrict__ sw,
-                                                 const float4 *__restrict__ ax_in, const float4 *__restrict__ av_in,
-                                                 float4 *__restrict__ ax_out, float4 *__restrict__ av_out,
-                                                 float *__restrict__ gmu, float *__restrict__ gmv,
-                                                 float *__restrict__ gmw, float *__restrict__ gsu,
-                                                 float *__restrict__ gsv, float *__restrict__ gsw,
-                                                 const uint8_t *__restrict__ mat) {
+// Fixed-point scale of one scatter pass: terms are rounded to multiples of inv = 2^-S.
+struct FixScale {
+    double scale, inv;   // 2^S, 2^-S (0 when there is nothing to scatter)
+    unsigned maxbits;    // largest |scatter value| of the pass, as float bits
+};
+
+// S = 61 - e - lg with max |value| < 2^e and at most 2^lg terms per node: every
+// term is below 2^(61 - lg) in magnitude, so no node sum leaves (-2^61, 2^61).
+// A value that is not finite sets *status and leaves the pass without a scatter.
+__global__ void k_fix_scale(FixScale *fs, int lg, unsigned *status) {
+    const unsigned b = fs->maxbits;
+    if (b == 0u || b >= 0x7f800000u) {
+        fs->scale = 0.0;
+        fs->inv = 0.0;
+        if (b) *status = 1u;
+        return;
+    }
+    const int e = (int)max(b >> 23, 1u) - 126;
+    const int S = 61 - e - lg;
+    fs->scale = __longlong_as_double((long long)(S + 1023) << 52);
+    fs->inv = __longlong_as_double((long long)(1023 - S) << 52);
+}
+
+__global__ void k_fix_unpack(const unsigned long long *__restrict__ acc, long long n, const FixScale *__restrict__ fs,
+                             float *__restrict__ out) {
     long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (q >= n) return;
+    if (q < n) out[q] = (float)((double)(long long)acc[q] * fs->inv);
+}
+
+// One particle of the G2P / RK4 adjoint.  SCALE_PASS: only the largest |value| the
+// particle scatters (float bits); otherwise the fixed-point scatter and the
+// per-particle adjoints.
+template <bool SCALE_PASS>
+__device__ __forceinline__ unsigned adj_g2p_particle(const AdvArgs &A, long long q, const float4 *__restrict__ pos,
+                                                     const float *__restrict__ mu, const float *__restrict__ mv,
+                                                     const float *__restrict__ mw, const float *__restrict__ su,
+                                                     const float *__restrict__ sv, const float *__restrict__ sw,
+                                                     const float4 *__restrict__ ax_in,
+                                                     const float4 *__restrict__ av_in, float4 *__restrict__ ax_out,
+                                                     float4 *__restrict__ av_out, unsigned long long *__restrict__ gmu,
+                                                     unsigned long long *__restrict__ gmv,
+                                                     unsigned long long *__restrict__ gmw,
+                                                     unsigned long long *__restrict__ gsu,
+                                                     unsigned long long *__restrict__ gsv,
+                                                     unsigned long long *__restrict__ gsw,
+                                                     const uint8_t *__restrict__ mat, double scale) {
+    unsigned mb = 0u;
+    auto scatter_velocity = [&](unsigned long long *gu, unsigned long long *gv, unsigned long long *gw, float px,
+                                float py, float pz, float3 c) {
+        if (SCALE_PASS)
+            mb = abs_bits_max(mb, c);
+        else
+            scatter_velocity_fixed(A, gu, gv, gw, px, py, pz, c, scale);
+    };
     const float4 P = pos[q];
     const uint32_t id = pid(P);
     const float4 XB = ax_in[id], VB = av_in[id];
@@ -237,32 +281,65 @@ __global__ void __launch_bounds__(128) k_adj_g2p(AdvArgs A, const float4 *__rest
     float3 kb1 = f3scale(xb_rk, A.f6), kb2 = f3scale(xb_rk, 2.0f * A.f6), kb3 = kb2, kb4 = kb1;
     {   // stage 4: k4 = u(y4), y4 = x + f1 k3
         float3 yb = mtv(J4, kb4);
-        scatter_velocity(A, gmu, gmv, gmw, y4.x, y4.y, y4.z, kb4);
+        scatter_velocity(gmu, gmv, gmw, y4.x, y4.y, y4.z, kb4);
         xbar = f3add(xbar, yb);
         kb3 = f3add(kb3, f3scale(yb, A.f1));
     }
     {   // stage 3: k3 = u(y3), y3 = x + h k2
         float3 yb = mtv(J3, kb3);
-        scatter_velocity(A, gmu, gmv, gmw, y3.x, y3.y, y3.z, kb3);
+        scatter_velocity(gmu, gmv, gmw, y3.x, y3.y, y3.z, kb3);
         xbar = f3add(xbar, yb);
         kb2 = f3add(kb2, f3scale(yb, A.h));
     }
     {   // stage 2: k2 = u(y2), y2 = x + h k1
         float3 yb = mtv(J2, kb2);
-        scatter_velocity(A, gmu, gmv, gmw, y2.x, y2.y, y2.z, kb2);
+        scatter_velocity(gmu, gmv, gmw, y2.x, y2.y, y2.z, kb2);
         xbar = f3add(xbar, yb);
         kb1 = f3add(kb1, f3scale(yb, A.h));
     }
     {   // stage 1 and the FLIP sample: k1 = a = u(x)
         float3 c = f3add(kb1, abar);
-        scatter_velocity(A, gmu, gmv, gmw, x.x, x.y, x.z, c);
+        scatter_velocity(gmu, gmv, gmw, x.x, x.y, x.z, c);
         xbar = f3add(xbar, mtv(Ja, c));
     }
-    scatter_velocity(A, gsu, gsv, gsw, x.x, x.y, x.z, sbar);
+    scatter_velocity(gsu, gsv, gsw, x.x, x.y, x.z, sbar);
+    if (SCALE_PASS) return mb;
     xbar = f3add(xbar, mtv(Js, sbar));
     ax_out[id] = make_float4(xbar.x, xbar.y, xbar.z, 0.f);
     float3 vbar = f3scale(vb, A.b_flip);
     av_out[id] = make_float4(vbar.x, vbar.y, vbar.z, 0.f);
+    return 0u;
+}
+
+// The G2P / RK4 adjoint, run twice: the scale pass finds the largest value the
+// launch scatters (k_fix_scale turns it into the fixed-point scale), the second
+// pass scatters in fixed point and writes the per-particle adjoints.  The
+// integer sums make the face-grid adjoints independent of particle order.
+template <bool SCALE_PASS>
+__global__ void __launch_bounds__(128) k_adj_g2p(AdvArgs A, const float4 *__restrict__ pos,
+                                                 const float4 *__restrict__ vel, long long n,
+                                                 const float *__restrict__ mu, const float *__restrict__ mv,
+                                                 const float *__restrict__ mw, const float *__restrict__ su,
+                                                 const float *__restrict__ sv, const float *__restrict__ sw,
+                                                 const float4 *__restrict__ ax_in, const float4 *__restrict__ av_in,
+                                                 float4 *__restrict__ ax_out, float4 *__restrict__ av_out,
+                                                 unsigned long long *__restrict__ gmu,
+                                                 unsigned long long *__restrict__ gmv,
+                                                 unsigned long long *__restrict__ gmw,
+                                                 unsigned long long *__restrict__ gsu,
+                                                 unsigned long long *__restrict__ gsv,
+                                                 unsigned long long *__restrict__ gsw,
+                                                 const uint8_t *__restrict__ mat, FixScale *__restrict__ fs) {
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const double scale = SCALE_PASS ? 0.0 : fs->scale;
+    unsigned mb = 0u;
+    if (q < n)
+        mb = adj_g2p_particle<SCALE_PASS>(A, q, pos, mu, mv, mw, su, sv, sw, ax_in, av_in, ax_out, av_out, gmu, gmv,
+                                          gmw, gsu, gsv, gsw, mat, scale);
+    if (SCALE_PASS) {
+        mb = __reduce_max_sync(0xffffffffu, mb);
+        if ((threadIdx.x & 31) == 0 && mb) atomicMax(&fs->maxbits, mb);
+    }
 }
 
 // ---------------------------------------------- 3. extrapolation adjoint
@@ -541,18 +618,36 @@ __global__ void __launch_bounds__(128) k_adj_p2g(AdjSplatArgs A, const float4 *_
     av[id] = make_float4(Vv.x + vb[0], Vv.y + vb[1], Vv.z + vb[2], 0.f);
 }
 
-// initial velocities: u0_bar = scatter of v_bar at the starting positions
+// initial velocities: u0_bar = scatter of v_bar at the starting positions, in
+// the same two passes as k_adj_g2p (scale, then fixed-point scatter)
+template <bool SCALE_PASS>
 __global__ void k_adj_sample(AdvArgs A, const float4 *__restrict__ pos, long long n, const float4 *__restrict__ av,
-                             float *__restrict__ gu, float *__restrict__ gv, float *__restrict__ gw) {
-    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (q >= n) return;
-    float4 P = pos[q];
-    float4 B = av[pid(P)];
-    scatter_velocity(A, gu, gv, gw, P.x, P.y, P.z, make_float3(B.x, B.y, B.z));
+                             unsigned long long *__restrict__ gu, unsigned long long *__restrict__ gv,
+                             unsigned long long *__restrict__ gw, FixScale *__restrict__ fs) {
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    unsigned mb = 0u;
+    if (q < n) {
+        const float4 P = pos[q];
+        const float4 B = av[pid(P)];
+        const float3 c = make_float3(B.x, B.y, B.z);
+        if (SCALE_PASS)
+            mb = abs_bits_max(mb, c);
+        else
+            scatter_velocity_fixed(A, gu, gv, gw, P.x, P.y, P.z, c, fs->scale);
+    }
+    if (SCALE_PASS) {
+        mb = __reduce_max_sync(0xffffffffu, mb);
+        if ((threadIdx.x & 31) == 0 && mb) atomicMax(&fs->maxbits, mb);
+    }
 }
 
-// sum of the particle positions into c[0..2] (FP64)
-__global__ void k_diff_centroid(const float4 *__restrict__ pos, long long n, double *__restrict__ c) {
+// Per-block sums of the particle positions (FP64) into part[3 * block + 0..2]:
+// a fixed grid, a fixed grid-stride split and fixed shuffle / shared-memory trees,
+// so the sums do not depend on scheduling.
+static constexpr int CENTROID_BLOCKS = 64, CENTROID_THREADS = 256;
+__global__ void __launch_bounds__(CENTROID_THREADS) k_diff_centroid(const float4 *__restrict__ pos, long long n,
+                                                                   double *__restrict__ part) {
+    __shared__ double sh[CENTROID_THREADS / 32][3];
     double sx = 0.0, sy = 0.0, sz = 0.0;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
         float4 P = pos[q];
@@ -565,16 +660,28 @@ __global__ void k_diff_centroid(const float4 *__restrict__ pos, long long n, dou
         sy += __shfl_down_sync(0xffffffffu, sy, o);
         sz += __shfl_down_sync(0xffffffffu, sz, o);
     }
+    const int warp = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
-        atomicAdd(c, sx);
-        atomicAdd(c + 1, sy);
-        atomicAdd(c + 2, sz);
+        sh[warp][0] = sx;
+        sh[warp][1] = sy;
+        sh[warp][2] = sz;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int w = 0; w < CENTROID_THREADS / 32; w++) t += sh[w][threadIdx.x];
+        part[3 * blockIdx.x + threadIdx.x] = t;
     }
 }
 
-__global__ void k_diff_centroid_out(const double *__restrict__ c, int count, double inv_n, float *__restrict__ out) {
-    int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < count) out[q] = (float)(c[q] * inv_n);
+// the centroid from the per-block sums, added in block order
+__global__ void k_diff_centroid_out(const double *__restrict__ part, int nblocks, double inv_n,
+                                    float *__restrict__ out) {
+    const int c = threadIdx.x;
+    if (c >= 3) return;
+    double t = 0.0;
+    for (int b = 0; b < nblocks; b++) t += part[3 * b + c];
+    out[c] = (float)(t * inv_n);
 }
 
 // x_bar += g_c / n for every particle present at one substep boundary (the
@@ -624,7 +731,10 @@ struct DiffRun {
     DevMem ax, av, bx, bv;           // adjoints by particle id
     DevMem g0[3], g1[3], g2[3], wsum[3], cnt[3], par[3];   // padded face grids
     DevMem pbar;                     // padded cells, double
-    DevMem cen;                      // (nsteps + 1) x 3 position sums, double
+    DevMem cen;                      // per-block position sums of one centroid, double
+    DevMem acc[6];                   // fixed-point face adjoints: MAC u v w, saved u v w
+    DevMem fix;                      // FixScale of the current scatter pass
+    DevMem status;                   // non-finite scatter values seen (unsigned)
     DevMem ckp;                      // nsteps x padded-cell pressure of every substep (double)
     bool sampled = true;             // initial velocities sampled from the parameter field
     std::vector<long long> count;    // particles at the start of every substep (and at the end)
@@ -634,11 +744,6 @@ struct DiffRun {
 
 static float4 *ck_pos(DiffRun *d, int step) { return d->ck.as<float4>() + (size_t)step * 2 * d->n; }
 static float4 *ck_vel(DiffRun *d, int step) { return d->ck.as<float4>() + ((size_t)step * 2 + 1) * d->n; }
-
-static int zero_faces(Ctx *ctx, DevMem m[3]) {
-    for (int q = 0; q < 3; q++) GFS_CUDA_CHECK(cudaMemsetAsync(m[q].p, 0, m[q].bytes, ctx->stream));
-    return GFS_OK;
-}
 
 static float *const *fptr(DevMem m[3], float *out[3]) {
     for (int q = 0; q < 3; q++) out[q] = m[q].as<float>();
@@ -657,7 +762,10 @@ static int diff_alloc(DiffRun *d) {
             if (m->alloc(fb)) return GFS_ERR_NOMEM;
     }
     if (d->pbar.alloc((size_t)g.c.size * sizeof(double))) return GFS_ERR_NOMEM;
-    if (d->cen.alloc((size_t)(d->nsteps + 1) * 3 * sizeof(double))) return GFS_ERR_NOMEM;
+    for (int q = 0; q < 6; q++)
+        if (d->acc[q].alloc((size_t)g.f[q % 3].size * sizeof(unsigned long long))) return GFS_ERR_NOMEM;
+    if (d->fix.alloc(sizeof(FixScale)) || d->status.alloc(sizeof(unsigned))) return GFS_ERR_NOMEM;
+    if (d->cen.alloc((size_t)CENTROID_BLOCKS * 3 * sizeof(double))) return GFS_ERR_NOMEM;
     if (d->ckp.alloc((size_t)d->nsteps * g.c.size * sizeof(double))) return GFS_ERR_NOMEM;
     GFS_CUDA_CHECK(cudaMemsetAsync(d->pbar.p, 0, d->pbar.bytes, s->ctx->stream));
     return GFS_OK;
@@ -752,7 +860,8 @@ void diff_info(DiffRun *d, double *fwd_ms, double *bwd_ms, long long *bytes) {
     if (bwd_ms) *bwd_ms = d->bwd_ms;
     if (bytes) {
         size_t b = d->ck.bytes + d->ckp.bytes + d->cen.bytes + d->ax.bytes + d->av.bytes + d->bx.bytes +
-                   d->bv.bytes + d->pbar.bytes;
+                   d->bv.bytes + d->pbar.bytes + d->fix.bytes + d->status.bytes;
+        for (int q = 0; q < 6; q++) b += d->acc[q].bytes;
         for (int q = 0; q < 3; q++)
             b += d->g0[q].bytes + d->g1[q].bytes + d->g2[q].bytes + d->wsum[q].bytes + d->cnt[q].bytes +
                  d->par[q].bytes;
@@ -824,10 +933,10 @@ int diff_forward(DiffRun *d, const float *d_pos, const float *d_vel0, const floa
         ctx->launches++;
     }
     if (d_centroids) {
-        GFS_CUDA_CHECK(cudaMemsetAsync(d->cen.p, 0, d->cen.bytes, st));
         for (int step = 0; step <= d->nsteps; step++) {
-            k_diff_centroid<<<64, 256, 0, st>>>(ck_pos(d, step), d->count[step], d->cen.as<double>() + 3 * step);
-            k_diff_centroid_out<<<1, 32, 0, st>>>(d->cen.as<double>() + 3 * step, 3, 1.0 / (double)d->count[step],
+            k_diff_centroid<<<CENTROID_BLOCKS, CENTROID_THREADS, 0, st>>>(ck_pos(d, step), d->count[step],
+                                                                         d->cen.as<double>());
+            k_diff_centroid_out<<<1, 32, 0, st>>>(d->cen.as<double>(), CENTROID_BLOCKS, 1.0 / (double)d->count[step],
                                                   d_centroids + 3 * step);
         }
         ctx->launches += 2 * (d->nsteps + 1);
@@ -842,6 +951,83 @@ int diff_forward(DiffRun *d, const float *d_pos, const float *d_vel0, const floa
     cudaEventDestroy(e1);
     d->have_forward = true;
     return GFS_OK;
+}
+
+static int ceil_log2(long long v) {
+    int l = 0;
+    while ((1LL << l) < v) l++;
+    return l;
+}
+
+// fixed-point sums acc[first .. first+count) -> float face grids out[0 .. count)
+static int fix_unpack(DiffRun *d, int first, int count, DevMem *out) {
+    cudaStream_t st = d->s->ctx->stream;
+    for (int q = 0; q < count; q++) {
+        const long long cnt = d->s->g.f[(first + q) % 3].size;
+        k_fix_unpack<<<grid_blocks(cnt, 256), 256, 0, st>>>(d->acc[first + q].as<unsigned long long>(), cnt,
+                                                            d->fix.as<FixScale>(), out[q].as<float>());
+    }
+    d->s->ctx->launches += count;
+    GFS_LAUNCH_CHECK();
+    return GFS_OK;
+}
+
+static int fix_begin(DiffRun *d, int count) {
+    cudaStream_t st = d->s->ctx->stream;
+    for (int q = 0; q < count; q++) GFS_CUDA_CHECK(cudaMemsetAsync(d->acc[q].p, 0, d->acc[q].bytes, st));
+    GFS_CUDA_CHECK(cudaMemsetAsync(d->fix.p, 0, d->fix.bytes, st));
+    return GFS_OK;
+}
+
+// k_adj_g2p's two passes over the m particles of a substep, then g0 / g1 from the sums
+static int adj_g2p(DiffRun *d, const AdvArgs &A, long long m, int lg) {
+    Sim *s = d->s;
+    cudaStream_t st = s->ctx->stream;
+    const int T = 128;
+    int rc;
+    if ((rc = fix_begin(d, 6))) return rc;
+    unsigned long long *a[6];
+    for (int q = 0; q < 6; q++) a[q] = d->acc[q].as<unsigned long long>();
+    FixScale *fs = d->fix.as<FixScale>();
+    const float *mac[3] = {s->mac[0].as<float>(), s->mac[1].as<float>(), s->mac[2].as<float>()};
+    const float *sav[3] = {s->saved[0].as<float>(), s->saved[1].as<float>(), s->saved[2].as<float>()};
+    if (m > 0) {
+        k_adj_g2p<true><<<grid_blocks(m, T), T, 0, st>>>(A, s->pos.as<float4>(), s->vel.as<float4>(), m, mac[0],
+                                                         mac[1], mac[2], sav[0], sav[1], sav[2], d->ax.as<float4>(),
+                                                         d->av.as<float4>(), d->bx.as<float4>(), d->bv.as<float4>(),
+                                                         a[0], a[1], a[2], a[3], a[4], a[5], s->mat.as<uint8_t>(), fs);
+        k_fix_scale<<<1, 1, 0, st>>>(fs, lg, d->status.as<unsigned>());
+        k_adj_g2p<false><<<grid_blocks(m, T), T, 0, st>>>(A, s->pos.as<float4>(), s->vel.as<float4>(), m, mac[0],
+                                                          mac[1], mac[2], sav[0], sav[1], sav[2], d->ax.as<float4>(),
+                                                          d->av.as<float4>(), d->bx.as<float4>(), d->bv.as<float4>(),
+                                                          a[0], a[1], a[2], a[3], a[4], a[5], s->mat.as<uint8_t>(), fs);
+        s->ctx->launches += 3;
+        GFS_LAUNCH_CHECK();
+    }
+    if ((rc = fix_unpack(d, 0, 3, d->g0))) return rc;
+    return fix_unpack(d, 3, 3, d->g1);
+}
+
+// k_adj_sample's two passes over the starting particles, then par from the sums
+static int adj_sample(DiffRun *d, const AdvArgs &A) {
+    Sim *s = d->s;
+    cudaStream_t st = s->ctx->stream;
+    const int T = 128;
+    int rc;
+    if ((rc = fix_begin(d, 3))) return rc;
+    unsigned long long *a[3];
+    for (int q = 0; q < 3; q++) a[q] = d->acc[q].as<unsigned long long>();
+    FixScale *fs = d->fix.as<FixScale>();
+    if (d->n > 0) {
+        k_adj_sample<true><<<grid_blocks(d->n, T), T, 0, st>>>(A, ck_pos(d, 0), d->n, d->av.as<float4>(), a[0],
+                                                               a[1], a[2], fs);
+        k_fix_scale<<<1, 1, 0, st>>>(fs, ceil_log2(d->n), d->status.as<unsigned>());
+        k_adj_sample<false><<<grid_blocks(d->n, T), T, 0, st>>>(A, ck_pos(d, 0), d->n, d->av.as<float4>(), a[0],
+                                                                a[1], a[2], fs);
+        s->ctx->launches += 3;
+        GFS_LAUNCH_CHECK();
+    }
+    return fix_unpack(d, 0, 3, d->par);
 }
 
 int diff_backward(DiffRun *d, const float *d_rho_bar, const float *d_grad_centroids, float *const d_grad[3],
@@ -861,6 +1047,7 @@ int diff_backward(DiffRun *d, const float *d_rho_bar, const float *d_grad_centro
     const int T = 128;
     const double R = DIFF_DENSITY_RADIUS * g.dx;
     // density adjoint at the final positions (ids removed earlier keep zero adjoints)
+    GFS_CUDA_CHECK(cudaMemsetAsync(d->status.p, 0, d->status.bytes, st));
     GFS_CUDA_CHECK(cudaMemsetAsync(d->ax.p, 0, d->ax.bytes, st));
     GFS_CUDA_CHECK(cudaMemsetAsync(d->av.p, 0, d->av.bytes, st));
     const long long mN = d->count[d->nsteps];
@@ -904,20 +1091,12 @@ int diff_backward(DiffRun *d, const float *d_rho_bar, const float *d_grad_centro
     for (int step = d->nsteps - 1; step >= 0; step--) {
         if ((rc = recompute(d, step, fptr(d->wsum, wp)))) return rc;
         const long long m = d->count[step];
-        // 2. G2P / RK4: g0 = MAC adjoint, g1 = saved adjoint; (bx, bv) by id, zero for
-        // ids not present in this substep
-        if ((rc = zero_faces(ctx, d->g0))) return rc;
-        if ((rc = zero_faces(ctx, d->g1))) return rc;
+        // 2. G2P / RK4: g0 = MAC adjoint, g1 = saved adjoint (from the fixed-point sums);
+        // (bx, bv) by id, zero for ids not present in this substep
         GFS_CUDA_CHECK(cudaMemsetAsync(d->bx.p, 0, d->bx.bytes, st));
         GFS_CUDA_CHECK(cudaMemsetAsync(d->bv.p, 0, d->bv.bytes, st));
-        k_adj_g2p<<<grid_blocks(m, T), T, 0, st>>>(
-            A, s->pos.as<float4>(), s->vel.as<float4>(), m, s->mac[0].as<float>(), s->mac[1].as<float>(),
-            s->mac[2].as<float>(), s->saved[0].as<float>(), s->saved[1].as<float>(), s->saved[2].as<float>(),
-            d->ax.as<float4>(), d->av.as<float4>(), d->bx.as<float4>(), d->bv.as<float4>(), d->g0[0].as<float>(),
-            d->g0[1].as<float>(), d->g0[2].as<float>(), d->g1[0].as<float>(), d->g1[1].as<float>(),
-            d->g1[2].as<float>(), s->mat.as<uint8_t>());
-        ctx->launches++;
-        GFS_LAUNCH_CHECK();
+        // a MAC node takes at most 4 terms per particle (the RK4 stages), a saved node 1
+        if ((rc = adj_g2p(d, A, m, ceil_log2(4 * m)))) return rc;
         // 3. extrapolations
         if ((rc = adj_extrapolate(d, d->g0, d->g2, layers))) return rc;
         if ((rc = adj_extrapolate(d, d->g1, d->g2, layers))) return rc;
@@ -978,15 +1157,12 @@ int diff_backward(DiffRun *d, const float *d_rho_bar, const float *d_grad_centro
     }
     if (d_grad[0] && d->sampled) {
         // the parameter field: u0_bar = scatter of v_bar at the starting positions
-        if ((rc = zero_faces(ctx, d->par))) return rc;
-        k_adj_sample<<<grid_blocks(d->n, T), T, 0, st>>>(A, ck_pos(d, 0), d->n, d->av.as<float4>(),
-                                                         d->par[0].as<float>(), d->par[1].as<float>(),
-                                                         d->par[2].as<float>());
+        if ((rc = adj_sample(d, A))) return rc;
         for (int q = 0; q < 3; q++) {
             dim3 grid(grid_blocks(g.f[q].nx, 128), g.f[q].ny, g.f[q].nz);
             k_diff_unpad<<<grid, 128, 0, st>>>(d->par[q].as<float>(), g.f[q], d_grad[q]);
         }
-        ctx->launches += 4;
+        ctx->launches += 3;
     }
     if (d_grad_pos0) {
         // with the initial velocities held fixed (their dependence on the
@@ -1002,6 +1178,12 @@ int diff_backward(DiffRun *d, const float *d_rho_bar, const float *d_grad_centro
     d->bwd_ms = ms;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    unsigned bad = 0;
+    GFS_CUDA_CHECK(cudaMemcpy(&bad, d->status.p, sizeof(bad), cudaMemcpyDeviceToHost));
+    if (bad) {
+        set_error(GFS_ERR_INVALID, "backward: an adjoint value is not finite (check the loss gradients)");
+        return GFS_ERR_INVALID;
+    }
     return GFS_OK;
 }
 

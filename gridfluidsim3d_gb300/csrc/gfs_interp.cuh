@@ -253,29 +253,6 @@ __device__ __forceinline__ float interp_component_grad(const float *__restrict__
     return acc;
 }
 
-// Transpose of interp_component: g[node] += weight(node) * c (atomically).
-__device__ __forceinline__ void scatter_component(float *__restrict__ g, const GridDim &f, float X, float Y, float Z,
-                                                  float c) {
-    if (c == 0.0f) return;
-    float fi = floorf(X), fj = floorf(Y), fk = floorf(Z);
-    int i = (int)fi, j = (int)fj, k = (int)fk;
-    float wx[4], wy[4], wz[4];
-    catmull_rom_weights(X - fi, wx);
-    catmull_rom_weights(Y - fj, wy);
-    catmull_rom_weights(Z - fk, wz);
-    const long long sy = f.sx, sz = (long long)f.sx * f.sy;
-    float *base = g + f.at(i - 1, j - 1, k - 1);
-#pragma unroll
-    for (int cc = 0; cc < 4; cc++)
-#pragma unroll
-        for (int b = 0; b < 4; b++) {
-            float wbc = wz[cc] * wy[b] * c;
-            float *row = base + b * sy + cc * sz;
-#pragma unroll
-            for (int a = 0; a < 4; a++) atomicAdd(row + a, wx[a] * wbc);
-        }
-}
-
 // Index-space coordinates of a world position (as eval_velocity forms them).
 __device__ __forceinline__ void to_index(const AdvArgs &A, float x, float y, float z, float &X, float &Y, float &Z) {
     if (A.pow2) {
@@ -315,15 +292,55 @@ __device__ __forceinline__ float3 eval_velocity_jac(const AdvArgs &A, const floa
     return make_float3(vx, vy, vz);
 }
 
-// Transpose of eval_velocity: adds c (a velocity adjoint) into the face grids.
-__device__ __forceinline__ void scatter_velocity(const AdvArgs &A, float *__restrict__ u, float *__restrict__ v,
-                                                 float *__restrict__ w, float x, float y, float z, float3 c) {
+// Transpose of interp_component in fixed point: g[node] += round(weight(node) * c * scale)
+// by 64-bit integer atomics.  Integer addition is associative, so the node sums do
+// not depend on the order in which the particles arrive.  |weight| <= 1 for
+// Catmull-Rom, so |term| <= |c| * scale; the caller picks scale (a power of two)
+// so that no node sum can leave the int64 range.
+__device__ __forceinline__ void scatter_component_fixed(unsigned long long *__restrict__ g, const GridDim &f, float X,
+                                                        float Y, float Z, float c, double scale) {
+    if (c == 0.0f || scale == 0.0) return;
+    float fi = floorf(X), fj = floorf(Y), fk = floorf(Z);
+    int i = (int)fi, j = (int)fj, k = (int)fk;
+    float wx[4], wy[4], wz[4];
+    catmull_rom_weights(X - fi, wx);
+    catmull_rom_weights(Y - fj, wy);
+    catmull_rom_weights(Z - fk, wz);
+    const long long sy = f.sx, sz = (long long)f.sx * f.sy;
+    unsigned long long *base = g + f.at(i - 1, j - 1, k - 1);
+#pragma unroll
+    for (int cc = 0; cc < 4; cc++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            float wbc = wz[cc] * wy[b] * c;
+            unsigned long long *row = base + b * sy + cc * sz;
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                long long t = __double2ll_rn((double)(wx[a] * wbc) * scale);
+                if (t) atomicAdd(row + a, (unsigned long long)t);
+            }
+        }
+}
+
+// Transpose of eval_velocity: adds c (a velocity adjoint) into fixed-point face grids.
+__device__ __forceinline__ void scatter_velocity_fixed(const AdvArgs &A, unsigned long long *__restrict__ u,
+                                                       unsigned long long *__restrict__ v,
+                                                       unsigned long long *__restrict__ w, float x, float y, float z,
+                                                       float3 c, double scale) {
     if (!inside(A, x, y, z)) return;
     float X, Y, Z;
     to_index(A, x, y, z, X, Y, Z);
-    scatter_component(u, A.f[0], X, Y - 0.5f, Z - 0.5f, c.x);
-    scatter_component(v, A.f[1], X - 0.5f, Y, Z - 0.5f, c.y);
-    scatter_component(w, A.f[2], X - 0.5f, Y - 0.5f, Z, c.z);
+    scatter_component_fixed(u, A.f[0], X, Y - 0.5f, Z - 0.5f, c.x, scale);
+    scatter_component_fixed(v, A.f[1], X - 0.5f, Y, Z - 0.5f, c.y, scale);
+    scatter_component_fixed(w, A.f[2], X - 0.5f, Y - 0.5f, Z, c.z, scale);
+}
+
+// The largest |component| of a scatter value, as float bits: for |x| the bit
+// patterns order like the values, and a NaN sorts above +inf.
+__device__ __forceinline__ unsigned abs_bits_max(unsigned m, float3 c) {
+    m = max(m, __float_as_uint(fabsf(c.x)));
+    m = max(m, __float_as_uint(fabsf(c.y)));
+    return max(m, __float_as_uint(fabsf(c.z)));
 }
 
 }  // namespace gfs
