@@ -413,7 +413,8 @@ class FluidSimulation:
                                   ctypes.byref(h))
         self._h = h
         self._dependents = weakref.WeakSet()   # rollouts built on this simulation
-        self.ctx._dependents.add(self)
+        if getattr(self.ctx, "_dependents", None) is not None:
+            self.ctx._dependents.add(self)
         self._params = SimParams()
         _lib.lib().gfs_sim_default_params(ctypes.byref(self._params))
         self.last_stats = None
