@@ -699,6 +699,120 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1) k_sweep(SweepArgs<T> A) {
     }
 }
 
+// ---------------------------------------------------- receiver warp
+//
+// The L2 hand-over between blocks.  A block's 32 upstream edge pencils (16 on
+// the j edge, 16 on the k edge) each need one exchange word per step from a
+// producer block.  Polled by the pencils themselves, a word that is not there
+// yet costs the whole block an L2 round trip per step; near a block's start,
+// where it runs just behind its producer, that is every step.  Instead, one
+// extra warp per block (the receiver) keeps RX_D reads in flight per edge pencil,
+// re-reads every pending step once per round, and publishes the words in a
+// shared ring: values, then the pencil's progress (all steps below it are in
+// the ring).  The compute threads read shared memory only, look at the
+// progress again only when the steps it covered are used up, and hand ring
+// slots back RX_CB steps at a time.
+static constexpr int RX_R = 32;    // ring steps per pencil
+static constexpr int RX_D = 4;     // reads in flight per pencil
+static constexpr int RX_CB = 8;    // slots handed back together
+static constexpr int RX_THREADS = 32;
+
+template <class T>
+struct RxRing {
+    T val[RX_R][32];
+    int prog[32];   // lane l: steps below prog[l] are in val
+    int cons[32];   // lane l: steps below cons[l] have been read
+};
+
+__device__ __forceinline__ int ld_volatile_s32(const int *p) { return *(const volatile int *)p; }
+__device__ __forceinline__ void st_volatile_s32(int *p, int v) { *(volatile int *)p = v; }
+
+// Receiver lane: steps [s_lo, s_hi) of one edge pencil, whose word of step s is
+// at src + s * xs.  A read that has not seen the tag after `limit` rounds marks
+// the timeout and publishes every step, so that no compute thread waits on it.
+template <class T>
+__device__ void rx_receive(RxRing<T> &R, int lane, const unsigned long long *src, long long xs, int s_lo, int s_hi,
+                           unsigned tag, int limit, PsCtrl *ctrl) {
+    using X = Xch<T>;
+    unsigned long long w[RX_D][X::W];
+    int sd[RX_D];
+    int next = s_lo, assign = s_lo;
+    unsigned mask = 0u;   // bit b: step next + b is in the ring
+#pragma unroll
+    for (int d = 0; d < RX_D; d++) {
+        sd[d] = -1;
+        if (assign < s_hi) {
+            sd[d] = assign;
+            X::fetch(src + (long long)assign * xs, w[d]);
+            assign++;
+        }
+    }
+    int rounds = 0;
+    while (next < s_hi) {
+        if (++rounds > limit) {
+            atomicOr(&ctrl->err, GFS_DEV_ERR_TIMEOUT);
+            __threadfence_block();
+            st_volatile_s32(&R.prog[lane], s_hi);
+            return;
+        }
+#pragma unroll
+        for (int d = 0; d < RX_D; d++) {
+            if (sd[d] >= 0) {
+                if (X::ready(w[d], tag)) {
+                    R.val[sd[d] & (RX_R - 1)][lane] = X::value(w[d]);
+                    mask |= 1u << (sd[d] - next);
+                    sd[d] = -1;
+                } else {
+                    X::fetch(src + (long long)sd[d] * xs, w[d]);
+                }
+            }
+        }
+        if (mask & 1u) {
+            while (mask & 1u) {
+                mask >>= 1;
+                next++;
+            }
+            __threadfence_block();   // the values before the progress
+            st_volatile_s32(&R.prog[lane], next);
+        }
+        const int room = max(ld_volatile_s32(&R.cons[lane]), s_lo) + RX_R;
+#pragma unroll
+        for (int d = 0; d < RX_D; d++) {
+            if (sd[d] < 0 && assign < s_hi && assign < room && assign - next < 32) {
+                sd[d] = assign;
+                X::fetch(src + (long long)assign * xs, w[d]);
+                assign++;
+            }
+        }
+    }
+}
+
+// Compute thread: the value of step st of receiver lane `lane` (st in [s_lo, s_hi)).
+template <class T>
+__device__ __forceinline__ T rx_ring_take(RxRing<T> &R, int lane, int st, int s_hi, int &seen, int limit,
+                                          PsCtrl *ctrl, bool &timed_out) {
+    if (st >= seen) {
+        int spins = 0;
+        while ((seen = ld_volatile_s32(&R.prog[lane])) <= st) {
+            if (timed_out || ++spins > limit) {
+                if (!timed_out) atomicOr(&ctrl->err, GFS_DEV_ERR_TIMEOUT);
+                timed_out = true;
+                seen = s_hi;
+                break;
+            }
+        }
+        __threadfence_block();   // the progress before the values
+    }
+    const T v = R.val[st & (RX_R - 1)][lane];
+    if (((st + 1) & (RX_CB - 1)) == 0 || st + 1 == s_hi) {
+        __threadfence_block();   // the read before the slot goes back
+        st_volatile_s32(&R.cons[lane], st + 1);
+    }
+    return v;
+}
+
+__device__ __forceinline__ void compute_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(SPLANE) : "memory"); }
+
 // Lean triangular solve (FWD / BWD).  One pencil per thread; everything that
 // does not depend on the step is hoisted, per-step addresses are pointer
 // increments, every slot of the block's plane is copied and stored (slots of
@@ -707,7 +821,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1) k_sweep(SweepArgs<T> A) {
 // being inside the grid.  This keeps the per-step instruction count -- the issue-rate limit of
 // the SMs hosting two such CTAs -- low.
 template <class T, int MODE, int P, int PE>
-__global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
+__global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) {
     using Op = Ar<T>;
     using X = Xch<T>;
     static_assert(MODE == SW_FWD || MODE == SW_BWD, "triangular solves only");
@@ -719,6 +833,7 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
     __shared__ T xb[2][SBK][SBJ];
     __shared__ __align__(16) T ring[NARR][P][SPLANE];
     __shared__ unsigned sh_ticket, sh_epoch;
+    __shared__ RxRing<T> rxr;
     if (A.ctrl->done) return;
     const int tid = threadIdx.x;
     const Skew &K = A.K;
@@ -726,6 +841,10 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
     if (tid == 0) {
         sh_ticket = atomicAdd(A.ticket, 1u);
         sh_epoch = A.ctrl->epoch;
+    }
+    if (tid < 32) {
+        rxr.prog[tid] = 0;
+        rxr.cons[tid] = 0;
     }
     __syncthreads();
     const unsigned t = sh_ticket, tag = sh_epoch;
@@ -744,7 +863,25 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
     const bool has_cj = cbj >= 0 && cbj < K.nbj && A.blkf[bk * K.nbj + cbj],
                has_ck = cbk >= 0 && cbk < K.nbk && A.blkf[cbk * K.nbj + bj];
     bool timed_out = false;
-
+    const long long xblock = (long long)S * XP;
+    Acc2f dot32;
+    double dot64 = 0.0;
+    if (tid >= SPLANE) {
+        // receiver warp: lane l < 16 feeds the j-edge pencil kl = l, lane 16 + l the k-edge pencil jl = l
+        const int lane = tid - SPLANE, e = lane >> 4, idx = lane & 15;
+        const int jl_c = e == 0 ? (bwd ? SBJ - 1 : 0) : idx, kl_c = e == 0 ? idx : (bwd ? SBK - 1 : 0);
+        const bool valid_c = live && bj * SBJ + jl_c < K.ny && bk * SBK + kl_c < K.nz;
+        if (valid_c && (e == 0 ? has_pj : has_pk)) {
+            const int lo = bwd ? S - K.nx - jl_c - kl_c : jl_c + kl_c;
+            const unsigned long long *src =
+                e == 0 ? A.xch + (long long)(bk * K.nbj + pbj) * xblock +
+                             (bwd ? (long long)(S - 1 - (SBJ - 1)) : (long long)(SBJ - 1)) * XP + (long long)idx * X::W
+                       : A.xch + (long long)(pbk * K.nbj + bj) * xblock +
+                             (bwd ? (long long)(S - 1 - (SBK - 1)) : (long long)(SBK - 1)) * XP +
+                             (long long)(SBJ + idx) * X::W;
+            rx_receive<T>(rxr, lane, src, XS, lo, lo + K.nx, wtag, A.spin_limit, A.ctrl);
+        }
+    } else {
     const int jl = tid % SBJ, kl = tid / SBJ;
     const bool valid = live && bj * SBJ + jl < K.ny && bk * SBK + kl < K.nz;
     const int xj = bwd ? jl + 1 : jl - 1, xk = bwd ? kl + 1 : kl - 1;
@@ -767,21 +904,12 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
     const T *ca = A.in + qp, *cb = A.precon + qp, *cc = (bwd ? A.rdot : A.in) + qp;
     const T *fa = ca + P * PS, *fb = cb + P * PS, *fc = cc + P * PS;   // the first refill: step P
     T *po = A.out + q0;
-    const long long xblock = (long long)S * XP;
     unsigned long long *xbuf = A.xch;
     unsigned long long *pxj_out = xbuf + (long long)(bk * K.nbj + bj) * xblock + (bwd ? (long long)(S - 1) * XP : 0) +
                                   (long long)kl * X::W;
     unsigned long long *pxk_out = xbuf + (long long)(bk * K.nbj + bj) * xblock + (bwd ? (long long)(S - 1) * XP : 0) +
                                   (long long)(SBJ + jl) * X::W;
-    const unsigned long long *pxj_in =
-        xbuf + (has_pj ? (long long)(bk * K.nbj + pbj) * xblock +
-                             (bwd ? (long long)(S - 1 - (SBJ - 1)) : (long long)(SBJ - 1)) * XP + (long long)kl * X::W
-                       : 0);
-    const unsigned long long *pxk_in =
-        xbuf + (has_pk ? (long long)(pbk * K.nbj + bj) * xblock +
-                             (bwd ? (long long)(S - 1 - (SBK - 1)) : (long long)(SBK - 1)) * XP +
-                             (long long)(SBJ + jl) * X::W
-                       : 0);
+    int seen_j = 0, seen_k = 0;   // receiver progress this thread has seen (j lane kl, k lane 16 + jl)
 
     // fill the ring with steps 0..P-1
 #pragma unroll
@@ -794,25 +922,14 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
         cp_async_commit();
     }
     cp_async_wait<P - 1>();   // step 0 has landed ...
-    __syncthreads();          // ... and is visible to every thread
-    unsigned long long r_wj[PE][X::W], r_wk[PE][X::W];
-#pragma unroll
-    for (int v = 0; v < PE; v++) {
-        const bool ok = v >= st_lo && v < st_hi;
-        if (in_j && ok) Xch<T>::fetch(pxj_in + v * XS, r_wj[v]);
-        if (in_k && ok) Xch<T>::fetch(pxk_in + v * XS, r_wk[v]);
-    }
+    compute_barrier();        // ... and is visible to every compute thread
 
     T prev = T(0);
-    Acc2f dot32;
-    double dot64 = 0.0;
-    static_assert(P % PE == 0, "exchange ring must divide the input ring");
     const int SP = live ? ((S + P - 1) / P) * P : 0;
     for (int s0 = 0; s0 < SP; s0 += P) {
 #pragma unroll
         for (int u = 0; u < P; u++) {
             const int st = s0 + u;
-            const int v = u % PE;
             // the slot step st-1 read is free (the barrier of step st-1 has passed):
             // refill it with step st-1+P
             if (copier && st >= 1) {   // warp-uniform: the other warps skip it
@@ -829,8 +946,8 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
             const bool act = st >= st_lo && st < st_hi;
             T nj_ = at_j ? T(0) : xb[(st - 1) & 1][kl][xj];
             T nk_ = at_k ? T(0) : xb[(st - 1) & 1][xk][jl];
-            if (in_j && act) nj_ = xch_take<T>(r_wj[v], pxj_in + (long long)st * XS, wtag, A.spin_limit, A.ctrl, timed_out);
-            if (in_k && act) nk_ = xch_take<T>(r_wk[v], pxk_in + (long long)st * XS, wtag, A.spin_limit, A.ctrl, timed_out);
+            if (in_j && act) nj_ = rx_ring_take<T>(rxr, kl, st, st_hi, seen_j, A.spin_limit, A.ctrl, timed_out);
+            if (in_k && act) nk_ = rx_ring_take<T>(rxr, SBJ + jl, st, st_hi, seen_k, A.spin_limit, A.ctrl, timed_out);
             const T ra = ring[0][u][tid], pc = ring[1][u][tid];
             T val, xch;
             if (MODE == SW_FWD) {
@@ -860,17 +977,12 @@ __global__ void __launch_bounds__(SPLANE, 1) k_tri(SweepArgs<T> A) {
             po += PS;
             xb[st & 1][kl][jl] = xch;
             prev = xch;
-            {
-                const int sx = st + PE;
-                const bool ok = sx >= st_lo && sx < st_hi;
-                if (in_j && ok) Xch<T>::fetch(pxj_in + (long long)sx * XS, r_wj[v]);
-                if (in_k && ok) Xch<T>::fetch(pxk_in + (long long)sx * XS, r_wk[v]);
-            }
             cp_async_wait<P - 2>();   // step st+1 has landed (its group is older than the last P-2)
-            __syncthreads();
+            compute_barrier();
         }
     }
     cp_async_wait<0>();
+    }
 
     double part = 0.0;
     if (MODE == SW_BWD) part = block_reduce<0>(sizeof(T) == 4 ? dot32.value() : dot64);
@@ -960,7 +1072,7 @@ __device__ __forceinline__ void rx_put(unsigned long long *p, T v, unsigned tag)
 __host__ __device__ __forceinline__ int rx_steps(int S) { return S - (SBJ - 1); }
 
 template <class T, int MODE, int P, int PE, int CL_J, int CL_K>
-__global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE, 1) k_tri_cl(SweepArgs<T> A) {
+__global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri_cl(SweepArgs<T> A) {
     namespace cg = cooperative_groups;
     using Op = Ar<T>;
     using X = Xch<T>;
@@ -975,6 +1087,7 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE, 1)
     __shared__ T xb[2][SBK][SBJ];
     __shared__ __align__(16) T ring[NARR][P][SPLANE];
     __shared__ unsigned sh_ticket, sh_epoch;
+    __shared__ RxRing<T> rxr;   // the L2 hand-overs (receiver warp)
     // receive buffers: j edge [step][kl][W], then k edge [step][jl][W]
     extern __shared__ __align__(16) unsigned long long rx[];
     if (A.ctrl->done) return;   // the same value in every block of the launch
@@ -985,7 +1098,11 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE, 1)
     const int S = K.S;
     const int NR = rx_steps(S);
     unsigned long long *rxj = rx, *rxk = rx + (long long)NR * SBK * W;
-    for (int q = tid; q < 2 * NR * SBK * W; q += SPLANE) rx[q] = 0ull;
+    for (int q = tid; q < 2 * NR * SBK * W; q += blockDim.x) rx[q] = 0ull;
+    if (tid < 32) {
+        rxr.prog[tid] = 0;
+        rxr.cons[tid] = 0;
+    }
     if (tid == 0) {
         if (rank == 0) sh_ticket = atomicAdd(A.ticket, 1u);
         sh_epoch = A.ctrl->epoch;
@@ -1013,17 +1130,34 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE, 1)
     const bool pj_cl = pbj >= j0 && pbj < j0 + CL_J, pk_cl = pbk >= k0 && pbk < k0 + CL_K;
     const bool cj_cl = cbj >= j0 && cbj < j0 + CL_J, ck_cl = cbk >= k0 && cbk < k0 + CL_K;
     bool timed_out = false;
-
+    const long long xblock = (long long)S * XP;
+    Acc2f dot32;
+    double dot64 = 0.0;
+    if (tid >= SPLANE) {
+        // receiver warp for the edges fed through L2: lane l < 16 feeds the j-edge
+        // pencil kl = l, lane 16 + l the k-edge pencil jl = l
+        const int lane = tid - SPLANE, e = lane >> 4, idx = lane & 15;
+        const int jl_c = e == 0 ? (bwd ? SBJ - 1 : 0) : idx, kl_c = e == 0 ? idx : (bwd ? SBK - 1 : 0);
+        const bool valid_c = live && bj * SBJ + jl_c < K.ny && bk * SBK + kl_c < K.nz;
+        if (valid_c && (e == 0 ? has_pj && !pj_cl : has_pk && !pk_cl)) {
+            const int lo = bwd ? S - K.nx - jl_c - kl_c : jl_c + kl_c;
+            const unsigned long long *src =
+                e == 0 ? A.xch + (long long)(bk * K.nbj + pbj) * xblock +
+                             (bwd ? (long long)(S - 1 - (SBJ - 1)) : (long long)(SBJ - 1)) * XP + (long long)idx * W
+                       : A.xch + (long long)(pbk * K.nbj + bj) * xblock +
+                             (bwd ? (long long)(S - 1 - (SBK - 1)) : (long long)(SBK - 1)) * XP +
+                             (long long)(SBJ + idx) * W;
+            rx_receive<T>(rxr, lane, src, XS, lo, lo + K.nx, wtag, A.spin_limit, A.ctrl);
+        }
+    } else {
     const int jl = tid % SBJ, kl = tid / SBJ;
     const bool valid = live && bj * SBJ + jl < K.ny && bk * SBK + kl < K.nz;
     const int xj = bwd ? jl + 1 : jl - 1, xk = bwd ? kl + 1 : kl - 1;
     const bool at_j = bwd ? jl == SBJ - 1 : jl == 0;
     const bool at_k = bwd ? kl == SBK - 1 : kl == 0;
     const bool in_j = at_j && has_pj, in_k = at_k && has_pk;
-    const bool in_jx = in_j && !pj_cl, in_kx = in_k && !pk_cl;   // through L2
     const bool out_j = (bwd ? jl == 0 : jl == SBJ - 1) && has_cj;
     const bool out_k = (bwd ? kl == 0 : kl == SBK - 1) && has_ck;
-    const bool out_jx = out_j && !cj_cl, out_kx = out_k && !ck_cl;
     const int st_lo = valid ? (bwd ? S - K.nx - jl - kl : jl + kl) : S;
     const int st_hi = valid ? st_lo + K.nx : S;
     const long long q0 = K.base(bj, bk) + kl * SBJ + jl + (bwd ? (long long)(S - 1) * SPLANE : 0);
@@ -1038,20 +1172,11 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE, 1)
     const T *ca = A.in + qp, *cb = A.precon + qp, *cc = (bwd ? A.rdot : A.in) + qp;
     const T *fa = ca + P * PS, *fb = cb + P * PS, *fc = cc + P * PS;
     T *po = A.out + q0;
-    const long long xblock = (long long)S * XP;
     unsigned long long *xbuf = A.xch;
     const long long bself = exists ? (long long)(bk * K.nbj + bj) * xblock : 0;
     unsigned long long *pxj_out = xbuf + bself + (bwd ? (long long)(S - 1) * XP : 0) + (long long)kl * W;
     unsigned long long *pxk_out = xbuf + bself + (bwd ? (long long)(S - 1) * XP : 0) + (long long)(SBJ + jl) * W;
-    const unsigned long long *pxj_in =
-        xbuf + (has_pj ? (long long)(bk * K.nbj + pbj) * xblock +
-                             (bwd ? (long long)(S - 1 - (SBJ - 1)) : (long long)(SBJ - 1)) * XP + (long long)kl * W
-                       : 0);
-    const unsigned long long *pxk_in =
-        xbuf + (has_pk ? (long long)(pbk * K.nbj + bj) * xblock +
-                             (bwd ? (long long)(S - 1 - (SBK - 1)) : (long long)(SBK - 1)) * XP +
-                             (long long)(SBJ + jl) * W
-                       : 0);
+    int seen_j = 0, seen_k = 0;   // receiver progress this thread has seen (j lane kl, k lane 16 + jl)
     // this thread's receive words (step 0) and, on a downstream edge inside the
     // cluster, the consumer's (its step 0 is this block's step SBJ-1)
     const unsigned long long *rj_in = rxj + (long long)kl * W;
@@ -1070,25 +1195,14 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE, 1)
         cp_async_commit();
     }
     cp_async_wait<P - 1>();   // step 0 has landed ...
-    __syncthreads();          // ... and is visible to every thread
-    unsigned long long r_wj[PE][W], r_wk[PE][W];
-#pragma unroll
-    for (int v = 0; v < PE; v++) {
-        const bool ok = v >= st_lo && v < st_hi;
-        if (in_jx && ok) X::fetch(pxj_in + v * XS, r_wj[v]);
-        if (in_kx && ok) X::fetch(pxk_in + v * XS, r_wk[v]);
-    }
+    compute_barrier();        // ... and is visible to every compute thread
 
     T prev = T(0);
-    Acc2f dot32;
-    double dot64 = 0.0;
-    static_assert(P % PE == 0, "exchange ring must divide the input ring");
     const int SP = live ? ((S + P - 1) / P) * P : 0;
     for (int s0 = 0; s0 < SP; s0 += P) {
 #pragma unroll
         for (int u = 0; u < P; u++) {
             const int st = s0 + u;
-            const int v = u % PE;
             // the slot step st-1 read is free (the barrier of step st-1 has passed):
             // refill it with step st-1+P
             if (copier && st >= 1) {   // warp-uniform: the other warps skip it
@@ -1107,10 +1221,10 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE, 1)
             T nk_ = at_k ? T(0) : xb[(st - 1) & 1][xk][jl];
             if (in_j && act)
                 nj_ = pj_cl ? rx_take<T>(rj_in + (long long)st * SBK * W, wtag, A.spin_limit, A.ctrl, timed_out)
-                            : xch_take<T>(r_wj[v], pxj_in + (long long)st * XS, wtag, A.spin_limit, A.ctrl, timed_out);
+                            : rx_ring_take<T>(rxr, kl, st, st_hi, seen_j, A.spin_limit, A.ctrl, timed_out);
             if (in_k && act)
                 nk_ = pk_cl ? rx_take<T>(rk_in + (long long)st * SBJ * W, wtag, A.spin_limit, A.ctrl, timed_out)
-                            : xch_take<T>(r_wk[v], pxk_in + (long long)st * XS, wtag, A.spin_limit, A.ctrl, timed_out);
+                            : rx_ring_take<T>(rxr, SBJ + jl, st, st_hi, seen_k, A.spin_limit, A.ctrl, timed_out);
             const T ra = ring[0][u][tid], pc = ring[1][u][tid];
             T val, xch;
             if (MODE == SW_FWD) {
@@ -1144,17 +1258,12 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE, 1)
             po += PS;
             xb[st & 1][kl][jl] = xch;
             prev = xch;
-            {
-                const int sx = st + PE;
-                const bool ok = sx >= st_lo && sx < st_hi;
-                if (in_jx && ok) X::fetch(pxj_in + (long long)sx * XS, r_wj[v]);
-                if (in_kx && ok) X::fetch(pxk_in + (long long)sx * XS, r_wk[v]);
-            }
             cp_async_wait<P - 2>();   // step st+1 has landed (its group is older than the last P-2)
-            __syncthreads();
+            compute_barrier();
         }
     }
     cp_async_wait<0>();
+    }
     // no block of the cluster leaves while a peer may still store into it
     cl.sync();
 
@@ -1652,7 +1761,7 @@ static bool tri_cl_usable(int S, int ncl) {
     if (active1 == 0) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(CJ * CK);
-        cfg.blockDim = dim3(SPLANE);
+        cfg.blockDim = dim3(SPLANE + RX_THREADS);
         cfg.dynamicSmemBytes = attr;
         int n = 0;
         if (cudaOccupancyMaxActiveClusters(&n, k_tri_cl<T, MODE, P, PE, CJ, CK>, &cfg) != cudaSuccess) n = 0;
@@ -1668,7 +1777,7 @@ static bool launch_tri_cl(Ctx *ctx, const SweepArgs<T> &A) {
     auto a16 = [](const void *q) { return ((uintptr_t)q & 15u) == 0; };
     if (!a16(A.in) || !a16(A.precon) || (MODE == SW_BWD && !a16(A.rdot))) return false;   // 16-byte copies
     if (!tri_cl_usable<T, MODE, P, PE, CJ, CK>(A.K.S, ncl)) return false;
-    k_tri_cl<T, MODE, P, PE, CJ, CK><<<ncl * CJ * CK, SPLANE, tri_cl_smem<T>(A.K.S), ctx->stream>>>(A);
+    k_tri_cl<T, MODE, P, PE, CJ, CK><<<ncl * CJ * CK, SPLANE + RX_THREADS, tri_cl_smem<T>(A.K.S), ctx->stream>>>(A);
     return true;
 }
 
@@ -1731,7 +1840,7 @@ static int launch_sweep(Ctx *ctx, PressureWs &ws, const T *in, T *out, const T *
                  launch_tri_cl<T, MODE, P, PE, 2, 2>(ctx, A))
             ran = GFS_SWEEP_CLUSTER_2X2;
         else if (want == GFS_SWEEP_AUTO || want == GFS_SWEEP_BLOCK) {
-            k_tri<T, MODE, P, PE><<<A.K.nbj * A.K.nbk, SPLANE, 0, ctx->stream>>>(A);
+            k_tri<T, MODE, P, PE><<<A.K.nbj * A.K.nbk, SPLANE + RX_THREADS, 0, ctx->stream>>>(A);
             ran = GFS_SWEEP_BLOCK;
         } else {
             set_error(GFS_ERR_INVALID, "sweep kernel %d cannot run this %dx%dx%d solve: its clusters do not all "
