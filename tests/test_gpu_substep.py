@@ -135,3 +135,42 @@ def test_pressure_check_against_fp64(gpu_ctx, precision):
         assert chk["fp64_residual"] < 1e-6
         assert chk["rel_error"] < (1e-6 if precision == "plain" else 1e-5), chk
     sim.close()
+
+
+@pytest.mark.parametrize("speed", [1.0, 40.0], ids=["slow", "fast"])
+def test_g2p_matches_standalone_sampler(gpu_ctx, speed):
+    """The substep's fused PIC/FLIP + RK4 pass and the drop-in ParticleAdvector
+    (RK4) and tricubic_interpolate on the step's own fields (the PIC/FLIP update
+    redone in float32 in the reference's operation order) give the same bits,
+    for every particle whose RK4 end point is not in a solid cell; the fast
+    scene moves particles several cells per substep."""
+    from gridfluidsim3d_gb300 import ParticleAdvector
+    sc = scenes.random_box(dims=(40, 24, 28), seed=6, vel_sigma=speed)
+    sim = FluidSimulation(*sc.dims, sc.dx, max_particles=sc.num_particles, ctx=gpu_ctx)
+    sim.set_material_grid(sc.mat)
+    sim.set_marker_particles(sc.pos, sc.vel, sc.ids)
+    sim.update(sc.dt)                                   # a substep, so the fields are not trivial
+    p0, v0, i0 = _by_id(*sim.get_marker_particles())
+    sim.update(sc.dt)
+    p1, v1, i1 = _by_id(*sim.get_marker_particles())
+    assert np.array_equal(i0, i1)
+    mac, saved = sim.get_velocity_field(), sim.get_saved_velocity_field()
+    adv = ParticleAdvector(gpu_ctx)
+    want = adv.advect_particles_rk4(p0, mac, sc.dt)
+    cell = np.floor(want.astype(np.float64) / sc.dx).astype(np.int64)
+    dims = np.array(sc.dims)
+    inside = np.all((cell >= 0) & (cell < dims), axis=1)
+    c = np.clip(cell, 0, dims - 1)
+    free = inside & (sc.mat[c[:, 2], c[:, 1], c[:, 0]] != 2)
+    assert free.mean() > 0.9
+    assert np.array_equal(p1[free], want[free])
+    vn = adv.tricubic_interpolate(p0, mac)
+    vo = adv.tricubic_interpolate(p0, saved)
+    a = np.float32(0.05)
+    b = np.float32(1.0) - a
+    vexp = a * vn + b * ((v0 + vn) - vo)
+    assert np.array_equal(v1, vexp)
+    if speed > 1.0:
+        disp = np.abs(want - p0).max(axis=1) / sc.dx
+        assert (disp > 2.0).sum() > 100
+    sim.close()
