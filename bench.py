@@ -658,9 +658,27 @@ def oracle_check(sim, sc, warmup, sample=400_000, seed=0):
     where[ids1] = np.arange(len(ids1))
     q = where[sid]
     kept = q >= 0
-    err = float(np.abs(pos1[q[kept]] - p_ref[kept]).max() / dx)
+    got, want = pos1[q[kept]], p_ref[kept]
+    d = np.abs(got - want)
+    err = float(d.max() / dx)
     vscale = max(float(np.abs(v_ref).max()), 1e-3)
+    # the per-substep position bars of the parity tests: 1e-5 cell + 4 float32 spacings of
+    # the coordinate (away from solid cells), 1e-5 cell + 16 spacings (every particle)
+    spacing = np.spacing(np.abs(want).astype(np.float32))
+    solid = np.pad(mat == 2, 1, constant_values=True)
+    near = np.zeros_like(solid)
+    for dk in (-1, 0, 1):
+        for dj in (-1, 0, 1):
+            for di in (-1, 0, 1):
+                near |= np.roll(solid, (dk, dj, di), axis=(0, 1, 2))
+    c = np.clip(np.floor(want.astype(np.float64) / dx).astype(np.int64) + 1, 0, np.array(near.shape[::-1]) - 1)
+    free = ~near[c[:, 2], c[:, 1], c[:, 0]]
+    tight = (d / (1e-5 * dx + 4 * spacing)).max(axis=1) > 1.0
+    loose = (d / (1e-5 * dx + 16 * spacing)).max(axis=1) > 1.0
     out["positions"] = {"sample": int(kept.sum()), "max_error_cells": err,
+                        "max_error_cells_away_from_solids": float(d[free].max() / dx) if free.any() else 0.0,
+                        "beyond_1e-5_cell_plus_4_spacings_away_from_solids": int((tight & free).sum()),
+                        "beyond_1e-5_cell_plus_16_spacings": int(loose.sum()),
                         "max_velocity_error_rel": float(np.abs(vel1[q[kept]] - v_ref[kept]).max() / vscale)}
     return out
 
@@ -941,7 +959,7 @@ def main(args):
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (particles, grids, MIC(0)/stencil); f64 dots + refinement residual",
             "data": "synthetic (seeded scene, no dataset)",
-            "config": {"workload": "slab_spheres 256^3 dx=1/32 + 20 spheres r~U(4,12) cells, 8 ppc, "
+            "config": {"workload": f"slab_spheres {SCENE['n']}^3 dx=8/{SCENE['n']} + 20 spheres r~U(4,12) cells, 8 ppc, "
                                    "v~N(0,0.5^2), dt=1/30, 1 substep per step",
                        "particles": int(st[0]["num_particles"]), "fluid_cells": int(F),
                        "precision": "mixed", "parallelism": f"replicas x{world}",
@@ -993,7 +1011,12 @@ def parse():
     ap.add_argument("--no-check", action="store_true", help="skip the per-step FP64 pressure check")
     ap.add_argument("--no-savestate", action="store_true", help="skip the savestate write/read leg")
     ap.add_argument("--no-configs", action="store_true", help="skip the 64^3 / 128^3 forward configurations")
+    ap.add_argument("--grid", type=int, default=256,
+                    help="grid size of the scene (the workload is 256; smaller grids are for small profiler captures)")
     a = ap.parse_args()
+    if a.grid != 256:
+        SCENE["n"] = a.grid
+        SCENE["dx"] = 8.0 / a.grid   # the same 8 m domain
     if a.warmup < 3:
         ap.error("--warmup must be >= 3")
     return a

@@ -705,23 +705,27 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1) k_sweep(SweepArgs<T> A) {
 // the j edge, 16 on the k edge) each need one exchange word per step from a
 // producer block.  Polled by the pencils themselves, a word that is not there
 // yet costs the whole block an L2 round trip per step; near a block's start,
-// where it runs just behind its producer, that is every step.  Instead, one
-// extra warp per block (the receiver) keeps RX_D reads in flight per edge pencil,
+// where it runs just behind its producer, that is every step, and the polling
+// branches and fences lengthen every step of the edge warps.  Instead, one extra
+// warp per block (the receiver) keeps RX_D reads in flight per edge pencil,
 // re-reads every pending step once per round, and publishes the words in a
-// shared ring: values, then the pencil's progress (all steps below it are in
-// the ring).  The compute threads read shared memory only, look at the
-// progress again only when the steps it covered are used up, and hand ring
-// slots back RX_CB steps at a time.
+// shared ring: values, then the pencil's progress (all steps below it are in the
+// ring).  Before the barrier that ends step st, warp 0 (the gate) waits until
+// every edge pencil's input of step st+1 is there -- in the ring, or for a
+// hand-over inside a thread-block cluster in the block's receive buffer -- so the
+// compute threads read their neighbours with plain loads, and the gate hands
+// ring slots back for all pencils together every RX_CB steps.
 static constexpr int RX_R = 32;    // ring steps per pencil
 static constexpr int RX_D = 4;     // reads in flight per pencil
-static constexpr int RX_CB = 8;    // slots handed back together
+static constexpr int RX_CB = 8;    // steps between slot hand-backs
 static constexpr int RX_THREADS = 32;
+static constexpr int RX_DONE = 0x7fffffff;   // progress of a pencil with nothing (more) to receive
 
 template <class T>
 struct RxRing {
     T val[RX_R][32];
     int prog[32];   // lane l: steps below prog[l] are in val
-    int cons[32];   // lane l: steps below cons[l] have been read
+    int cons;       // steps below cons have been read by the compute threads
 };
 
 __device__ __forceinline__ int ld_volatile_s32(const int *p) { return *(const volatile int *)p; }
@@ -729,7 +733,8 @@ __device__ __forceinline__ void st_volatile_s32(int *p, int v) { *(volatile int 
 
 // Receiver lane: steps [s_lo, s_hi) of one edge pencil, whose word of step s is
 // at src + s * xs.  A read that has not seen the tag after `limit` rounds marks
-// the timeout and publishes every step, so that no compute thread waits on it.
+// the timeout; either way the lane ends by publishing RX_DONE, so that the gate
+// never waits on it again.
 template <class T>
 __device__ void rx_receive(RxRing<T> &R, int lane, const unsigned long long *src, long long xs, int s_lo, int s_hi,
                            unsigned tag, int limit, PsCtrl *ctrl) {
@@ -738,6 +743,7 @@ __device__ void rx_receive(RxRing<T> &R, int lane, const unsigned long long *src
     int sd[RX_D];
     int next = s_lo, assign = s_lo;
     unsigned mask = 0u;   // bit b: step next + b is in the ring
+    st_volatile_s32(&R.prog[lane], s_lo);
 #pragma unroll
     for (int d = 0; d < RX_D; d++) {
         sd[d] = -1;
@@ -751,9 +757,7 @@ __device__ void rx_receive(RxRing<T> &R, int lane, const unsigned long long *src
     while (next < s_hi) {
         if (++rounds > limit) {
             atomicOr(&ctrl->err, GFS_DEV_ERR_TIMEOUT);
-            __threadfence_block();
-            st_volatile_s32(&R.prog[lane], s_hi);
-            return;
+            break;
         }
 #pragma unroll
         for (int d = 0; d < RX_D; d++) {
@@ -775,7 +779,7 @@ __device__ void rx_receive(RxRing<T> &R, int lane, const unsigned long long *src
             __threadfence_block();   // the values before the progress
             st_volatile_s32(&R.prog[lane], next);
         }
-        const int room = max(ld_volatile_s32(&R.cons[lane]), s_lo) + RX_R;
+        const int room = max(ld_volatile_s32(&R.cons), s_lo) + RX_R - RX_CB;
 #pragma unroll
         for (int d = 0; d < RX_D; d++) {
             if (sd[d] < 0 && assign < s_hi && assign < room && assign - next < 32) {
@@ -785,30 +789,42 @@ __device__ void rx_receive(RxRing<T> &R, int lane, const unsigned long long *src
             }
         }
     }
+    __threadfence_block();
+    st_volatile_s32(&R.prog[lane], RX_DONE);
 }
 
-// Compute thread: the value of step st of receiver lane `lane` (st in [s_lo, s_hi)).
+// Gate (warp 0, lane l for edge pencil l): wait until the input of step `need` of
+// every edge pencil is readable -- L2 pencils: the receiver's progress is past it
+// (cached in `seen`); cluster pencils: the tagged word is in the receive buffer
+// (rxw: the word of step 0, stride rxs words per step); pencils that need nothing
+// at `need` pass.  Bounded; a timeout marks the error and lets every later gate pass.
 template <class T>
-__device__ __forceinline__ T rx_ring_take(RxRing<T> &R, int lane, int st, int s_hi, int &seen, int limit,
-                                          PsCtrl *ctrl, bool &timed_out) {
-    if (st >= seen) {
-        int spins = 0;
-        while ((seen = ld_volatile_s32(&R.prog[lane])) <= st) {
-            if (timed_out || ++spins > limit) {
-                if (!timed_out) atomicOr(&ctrl->err, GFS_DEV_ERR_TIMEOUT);
-                timed_out = true;
-                seen = s_hi;
-                break;
+__device__ __forceinline__ void rx_gate(RxRing<T> &R, int lane, int need, bool l2, bool cl, int lo, int hi,
+                                        const unsigned long long *rxw, long long rxs, unsigned tag, int &seen,
+                                        int limit, PsCtrl *ctrl, bool &timed_out) {
+    using X = Xch<T>;
+    const bool wants = need >= lo && need < hi;
+    int spins = 0;
+    for (;;) {
+        bool ok = true;
+        if (wants && !timed_out) {
+            if (l2 && need >= seen) {
+                seen = ld_volatile_s32(&R.prog[lane]);
+                ok = need < seen;
+            } else if (cl) {
+                unsigned long long w[X::W];
+#pragma unroll
+                for (int q = 0; q < X::W; q++) w[q] = *(const volatile unsigned long long *)(rxw + need * rxs + q);
+                ok = X::ready(w, tag);
             }
         }
-        __threadfence_block();   // the progress before the values
+        if (__all_sync(0xffffffffu, ok)) break;
+        if (++spins > limit) {
+            if (!timed_out && lane == 0) atomicOr(&ctrl->err, GFS_DEV_ERR_TIMEOUT);
+            timed_out = true;
+        }
     }
-    const T v = R.val[st & (RX_R - 1)][lane];
-    if (((st + 1) & (RX_CB - 1)) == 0 || st + 1 == s_hi) {
-        __threadfence_block();   // the read before the slot goes back
-        st_volatile_s32(&R.cons[lane], st + 1);
-    }
-    return v;
+    __threadfence_block();   // what the gate saw before the barrier that follows
 }
 
 __device__ __forceinline__ void compute_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(SPLANE) : "memory"); }
@@ -842,10 +858,8 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
         sh_ticket = atomicAdd(A.ticket, 1u);
         sh_epoch = A.ctrl->epoch;
     }
-    if (tid < 32) {
-        rxr.prog[tid] = 0;
-        rxr.cons[tid] = 0;
-    }
+    if (tid < 32) rxr.prog[tid] = 0;
+    if (tid == 0) rxr.cons = 0;
     __syncthreads();
     const unsigned t = sh_ticket, tag = sh_epoch;
     const unsigned wtag = tag + A.wait_skew;   // the tag the waits look for (tag itself unless a test skews it)
@@ -909,7 +923,14 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
                                   (long long)kl * X::W;
     unsigned long long *pxk_out = xbuf + (long long)(bk * K.nbj + bj) * xblock + (bwd ? (long long)(S - 1) * XP : 0) +
                                   (long long)(SBJ + jl) * X::W;
-    int seen_j = 0, seen_k = 0;   // receiver progress this thread has seen (j lane kl, k lane 16 + jl)
+    // warp 0 is the gate: lane l watches edge pencil l (lanes 0-15 the j edge, kl = l;
+    // lanes 16-31 the k edge, jl = l - 16), all of them fed through L2 here
+    const int g_e = tid >> 4, g_idx = tid & 15;
+    const int g_jl = g_e == 0 ? (bwd ? SBJ - 1 : 0) : g_idx, g_kl = g_e == 0 ? g_idx : (bwd ? SBK - 1 : 0);
+    const bool g_valid = tid < 32 && live && bj * SBJ + g_jl < K.ny && bk * SBK + g_kl < K.nz;
+    const bool g_l2 = g_valid && (g_e == 0 ? has_pj : has_pk);
+    const int g_lo = bwd ? S - K.nx - g_jl - g_kl : g_jl + g_kl, g_hi = g_lo + K.nx;
+    int g_seen = 0;
 
     // fill the ring with steps 0..P-1
 #pragma unroll
@@ -922,7 +943,9 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
         cp_async_commit();
     }
     cp_async_wait<P - 1>();   // step 0 has landed ...
-    compute_barrier();        // ... and is visible to every compute thread
+    if (tid < 32 && live)
+        rx_gate<T>(rxr, tid, 0, g_l2, false, g_lo, g_hi, nullptr, 0, wtag, g_seen, A.spin_limit, A.ctrl, timed_out);
+    compute_barrier();        // ... and, with the edge inputs of step 0, is visible to every compute thread
 
     T prev = T(0);
     const int SP = live ? ((S + P - 1) / P) * P : 0;
@@ -946,8 +969,8 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
             const bool act = st >= st_lo && st < st_hi;
             T nj_ = at_j ? T(0) : xb[(st - 1) & 1][kl][xj];
             T nk_ = at_k ? T(0) : xb[(st - 1) & 1][xk][jl];
-            if (in_j && act) nj_ = rx_ring_take<T>(rxr, kl, st, st_hi, seen_j, A.spin_limit, A.ctrl, timed_out);
-            if (in_k && act) nk_ = rx_ring_take<T>(rxr, SBJ + jl, st, st_hi, seen_k, A.spin_limit, A.ctrl, timed_out);
+            if (in_j && act) nj_ = rxr.val[st & (RX_R - 1)][kl];         // the gate saw it arrive
+            if (in_k && act) nk_ = rxr.val[st & (RX_R - 1)][SBJ + jl];
             const T ra = ring[0][u][tid], pc = ring[1][u][tid];
             T val, xch;
             if (MODE == SW_FWD) {
@@ -978,6 +1001,12 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
             xb[st & 1][kl][jl] = xch;
             prev = xch;
             cp_async_wait<P - 2>();   // step st+1 has landed (its group is older than the last P-2)
+            if (tid < 32) {
+                if (st + 1 < S)
+                    rx_gate<T>(rxr, tid, st + 1, g_l2, false, g_lo, g_hi, nullptr, 0, wtag, g_seen, A.spin_limit,
+                               A.ctrl, timed_out);
+                if (tid == 0 && ((st + 1) & (RX_CB - 1)) == 0) st_volatile_s32(&rxr.cons, st);   // steps < st are read
+            }
             compute_barrier();
         }
     }
@@ -1027,33 +1056,22 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
 // of CL_J x CL_K blocks takes one dispatch ticket (clusters in dependency
 // order, 4 x 2 or 2 x 2 blocks); within it, a producer block stores each edge value, tagged as in the
 // L2 exchange, straight into the consumer block's shared receive buffer, where
-// the consumer polls its own shared memory.  Hand-overs between clusters keep
-// the L2 exchange words.  On a monotone path through the 16 x 16 blocks of a
+// the consumer block's gate warp checks the tag in its own shared memory.  Hand-overs between clusters go
+// through L2 and the receiver warp.  On a monotone path through the 16 x 16 blocks of a
 // 256^3 grid that leaves 3 + 7 (4 x 2) or 7 + 7 (2 x 2) of the 30 hand-overs in L2.  The receive
 // buffers hold every step (no slot is reused within a launch), so producers
 // need no flow control; a cluster barrier after zeroing them orders the first
 // remote store after the zeroing, and one before exit keeps every block
 // resident while its peers may still store into it.  Arithmetic, summation
 // order and outputs are k_tri's.
+
+// A receive-buffer word whose tag has been seen (by the gate).
 template <class T>
-__device__ __forceinline__ T rx_take(const unsigned long long *p, unsigned tag, int limit, PsCtrl *ctrl,
-                                     bool &timed_out) {
+__device__ __forceinline__ T rx_read(const unsigned long long *p) {
     using X = Xch<T>;
     unsigned long long w[X::W];
 #pragma unroll
     for (int q = 0; q < X::W; q++) w[q] = *(const volatile unsigned long long *)(p + q);
-    if (!X::ready(w, tag) && !timed_out) {
-        int spins = 0;
-        do {
-#pragma unroll
-            for (int q = 0; q < X::W; q++) w[q] = *(const volatile unsigned long long *)(p + q);
-            if (++spins > limit) {
-                atomicOr(&ctrl->err, GFS_DEV_ERR_TIMEOUT);
-                timed_out = true;
-                break;
-            }
-        } while (!X::ready(w, tag));
-    }
     return X::value(w);
 }
 
@@ -1099,10 +1117,8 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE + R
     const int NR = rx_steps(S);
     unsigned long long *rxj = rx, *rxk = rx + (long long)NR * SBK * W;
     for (int q = tid; q < 2 * NR * SBK * W; q += blockDim.x) rx[q] = 0ull;
-    if (tid < 32) {
-        rxr.prog[tid] = 0;
-        rxr.cons[tid] = 0;
-    }
+    if (tid < 32) rxr.prog[tid] = 0;
+    if (tid == 0) rxr.cons = 0;
     if (tid == 0) {
         if (rank == 0) sh_ticket = atomicAdd(A.ticket, 1u);
         sh_epoch = A.ctrl->epoch;
@@ -1176,7 +1192,17 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE + R
     const long long bself = exists ? (long long)(bk * K.nbj + bj) * xblock : 0;
     unsigned long long *pxj_out = xbuf + bself + (bwd ? (long long)(S - 1) * XP : 0) + (long long)kl * W;
     unsigned long long *pxk_out = xbuf + bself + (bwd ? (long long)(S - 1) * XP : 0) + (long long)(SBJ + jl) * W;
-    int seen_j = 0, seen_k = 0;   // receiver progress this thread has seen (j lane kl, k lane 16 + jl)
+    // warp 0 is the gate: lane l watches edge pencil l (lanes 0-15 the j edge, kl = l;
+    // lanes 16-31 the k edge, jl = l - 16), fed through L2 or, inside the cluster,
+    // through this block's receive buffer
+    const int g_e = tid >> 4, g_idx = tid & 15;
+    const int g_jl = g_e == 0 ? (bwd ? SBJ - 1 : 0) : g_idx, g_kl = g_e == 0 ? g_idx : (bwd ? SBK - 1 : 0);
+    const bool g_valid = tid < 32 && live && bj * SBJ + g_jl < K.ny && bk * SBK + g_kl < K.nz;
+    const bool g_has = g_valid && (g_e == 0 ? has_pj : has_pk), g_incl = g_e == 0 ? pj_cl : pk_cl;
+    const bool g_l2 = g_has && !g_incl, g_cl = g_has && g_incl;
+    const int g_lo = bwd ? S - K.nx - g_jl - g_kl : g_jl + g_kl, g_hi = g_lo + K.nx;
+    const unsigned long long *g_rxw = (g_e == 0 ? rxj : rxk) + (long long)g_idx * W;
+    int g_seen = 0;
     // this thread's receive words (step 0) and, on a downstream edge inside the
     // cluster, the consumer's (its step 0 is this block's step SBJ-1)
     const unsigned long long *rj_in = rxj + (long long)kl * W;
@@ -1195,7 +1221,10 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE + R
         cp_async_commit();
     }
     cp_async_wait<P - 1>();   // step 0 has landed ...
-    compute_barrier();        // ... and is visible to every compute thread
+    if (tid < 32 && live)
+        rx_gate<T>(rxr, tid, 0, g_l2, g_cl, g_lo, g_hi, g_rxw, (long long)SBK * W, wtag, g_seen, A.spin_limit, A.ctrl,
+                   timed_out);
+    compute_barrier();        // ... and, with the edge inputs of step 0, is visible to every compute thread
 
     T prev = T(0);
     const int SP = live ? ((S + P - 1) / P) * P : 0;
@@ -1219,12 +1248,11 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE + R
             const bool act = st >= st_lo && st < st_hi;
             T nj_ = at_j ? T(0) : xb[(st - 1) & 1][kl][xj];
             T nk_ = at_k ? T(0) : xb[(st - 1) & 1][xk][jl];
+            // the gate saw these inputs arrive
             if (in_j && act)
-                nj_ = pj_cl ? rx_take<T>(rj_in + (long long)st * SBK * W, wtag, A.spin_limit, A.ctrl, timed_out)
-                            : rx_ring_take<T>(rxr, kl, st, st_hi, seen_j, A.spin_limit, A.ctrl, timed_out);
+                nj_ = pj_cl ? rx_read<T>(rj_in + (long long)st * SBK * W) : rxr.val[st & (RX_R - 1)][kl];
             if (in_k && act)
-                nk_ = pk_cl ? rx_take<T>(rk_in + (long long)st * SBJ * W, wtag, A.spin_limit, A.ctrl, timed_out)
-                            : rx_ring_take<T>(rxr, SBJ + jl, st, st_hi, seen_k, A.spin_limit, A.ctrl, timed_out);
+                nk_ = pk_cl ? rx_read<T>(rk_in + (long long)st * SBJ * W) : rxr.val[st & (RX_R - 1)][SBJ + jl];
             const T ra = ring[0][u][tid], pc = ring[1][u][tid];
             T val, xch;
             if (MODE == SW_FWD) {
@@ -1259,6 +1287,12 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE + R
             xb[st & 1][kl][jl] = xch;
             prev = xch;
             cp_async_wait<P - 2>();   // step st+1 has landed (its group is older than the last P-2)
+            if (tid < 32) {
+                if (st + 1 < S)
+                    rx_gate<T>(rxr, tid, st + 1, g_l2, g_cl, g_lo, g_hi, g_rxw, (long long)SBK * W, wtag, g_seen,
+                               A.spin_limit, A.ctrl, timed_out);
+                if (tid == 0 && ((st + 1) & (RX_CB - 1)) == 0) st_volatile_s32(&rxr.cons, st);   // steps < st are read
+            }
             compute_barrier();
         }
     }
@@ -1834,10 +1868,11 @@ static int launch_sweep(Ctx *ctx, PressureWs &ws, const T *in, T *out, const T *
     } else {
         const int want = ctx->sweep_kernel;
         int ran = 0;
-        if ((want == GFS_SWEEP_AUTO || want == GFS_SWEEP_CLUSTER_4X2) && launch_tri_cl<T, MODE, P, PE, 4, 2>(ctx, A))
+        // AUTO: the block kernel, the fastest of the three with the receiver warp and gate
+        // (at 256^3 0.24 ms per FP32 backward solve against 0.28 for either cluster shape)
+        if (want == GFS_SWEEP_CLUSTER_4X2 && launch_tri_cl<T, MODE, P, PE, 4, 2>(ctx, A))
             ran = GFS_SWEEP_CLUSTER_4X2;
-        else if ((want == GFS_SWEEP_AUTO || want == GFS_SWEEP_CLUSTER_2X2) &&
-                 launch_tri_cl<T, MODE, P, PE, 2, 2>(ctx, A))
+        else if (want == GFS_SWEEP_CLUSTER_2X2 && launch_tri_cl<T, MODE, P, PE, 2, 2>(ctx, A))
             ran = GFS_SWEEP_CLUSTER_2X2;
         else if (want == GFS_SWEEP_AUTO || want == GFS_SWEEP_BLOCK) {
             k_tri<T, MODE, P, PE><<<A.K.nbj * A.K.nbk, SPLANE + RX_THREADS, 0, ctx->stream>>>(A);

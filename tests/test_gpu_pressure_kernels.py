@@ -87,11 +87,12 @@ def test_kernels_match_oracle_and_each_other(kernel_ctx, oracle_lib, system, pre
         assert np.array_equal(p, base_p), f"{name} differs from the block kernel"
 
 
-def test_auto_picks_a_cluster_kernel(kernel_ctx, system):
+def test_auto_runs_the_block_kernel(kernel_ctx, system):
     sc, mat, uvw, _, _ = system
     kernel_ctx.set_sweep_kernel(SWEEP_AUTO)
-    _solve(kernel_ctx, sc, mat, uvw, PRECISION_MIXED)
-    assert kernel_ctx.last_sweep_kernel() in (SWEEP_CLUSTER_4X2, SWEEP_CLUSTER_2X2)
+    for precision in (PRECISION_MIXED, PRECISION_PLAIN):
+        _solve(kernel_ctx, sc, mat, uvw, precision)
+        assert kernel_ctx.last_sweep_kernel() == SWEEP_BLOCK
 
 
 def test_invalid_kernel_is_rejected(kernel_ctx):
