@@ -85,7 +85,7 @@ BYTES = {
 # of the 5th/6th k_tri_cl launches of this bench's mixed run.  A sweep streams every
 # plane of each block that holds fluid (134 of the 256 blocks here), air and
 # padding slots included.
-TRAFFIC = {"mic0_forward": 91.3e6, "mic0_backward": 135.0e6}
+TRAFFIC = {"mic0_forward": 97.1e6, "mic0_backward": 143.2e6}
 
 
 def rank_info():
