@@ -10,7 +10,10 @@ no GPU involved:
   without fluid, both sweep directions and both cluster shapes;
 - a ring slot holds the step that reads it, its copy group has completed before
   the barrier that precedes the read, and it is refilled only after its last
-  read.
+  read;
+- the receiver warp's shared ring and the gate (L2 hand-overs): no slot is
+  overwritten before it is read, every read finds its own step, and no wait is
+  left without its value, under random producer and load timing.
 
 The wavefront itself follows pressuresolver.cpp:304-386 (forward / backward
 solve); its numerics are checked on the GPU against the oracle.
@@ -140,3 +143,106 @@ def ring_schedule(s_planes, p):
 def test_ring_refill_order(p):
     for s_planes in itertools.chain(range(1, 40), (286, 301, 542)):
         ring_schedule(s_planes, p)
+
+
+# ----------------------------------------------------------------------------
+# The receiver warp and the gate (csrc/pressure.cu rx_receive, rx_gate, k_tri):
+# a discrete-time restatement with random producer and load timing.  Each tick
+# every receiver lane runs one round (completed loads that see the step's word
+# publish it into ring slot step % RX_R, the others are reissued, progress is
+# published, free load slots take the next steps within room = max(cons, lo) +
+# RX_R - RX_CB); the compute threads run step st once the gate has seen every
+# lane's progress past st (for lanes active at st), read ring slot st % RX_R, and
+# every RX_CB steps hand back the slots below st.  Checked: no slot is written
+# while it holds a step not yet read, every read finds its own step's value, and
+# the sweep ends within a bounded number of ticks (no circular wait), for lanes
+# with different active ranges (forward and backward) and lanes without a producer.
+
+RX_R, RX_D, RX_CB = 32, 4, 8
+
+
+def rx_emulate(s_planes, lanes, seed):
+    """lanes: list of (lo, hi) active step ranges, or None for a lane without a
+    producer.  Returns the number of ticks the sweep took."""
+    rnd = random.Random(seed)
+    # the producer's word of step s (for lane l) becomes visible at tick avail[l][s]
+    avail = []
+    for rng in lanes:
+        a = {}
+        if rng is not None:
+            t = rnd.randrange(0, 6)
+            for s in range(rng[0], rng[1]):
+                t += rnd.choice((0, 0, 1, 1, 2, 5))
+                a[s] = t
+        avail.append(a)
+    ring = {}                   # slot -> (lane -> step it holds)
+    prog = [0] * len(lanes)
+    cons = 0
+    st_lanes = []
+    for l, rng in enumerate(lanes):
+        if rng is None:
+            st_lanes.append(None)
+            continue
+        lo, hi = rng
+        st_lanes.append({"next": lo, "assign": lo, "mask": 0, "sd": [None] * RX_D, "issued": [0] * RX_D})
+        prog[l] = lo
+    tick, st = 0, 0
+    limit = 50 * (s_planes + 100)
+    while st < s_planes:
+        tick += 1
+        assert tick < limit, "the sweep did not finish: a wait that never ends"
+        # receiver lanes: one round each
+        for l, rng in enumerate(lanes):
+            L = st_lanes[l]
+            if L is None or L["next"] >= rng[1]:
+                continue
+            lo, hi = rng
+            for d in range(RX_D):
+                s = L["sd"][d]
+                if s is None:
+                    continue
+                if avail[l][s] <= L["issued"][d]:          # the load saw the word
+                    slot = s % RX_R
+                    held = ring.setdefault(slot, {}).get(l)
+                    assert held is None or held < cons, (l, s, held, cons)   # its step was read
+                    ring[slot][l] = s
+                    L["mask"] |= 1 << (s - L["next"])
+                    L["sd"][d] = None
+                else:
+                    L["issued"][d] = tick                  # reissue
+            while L["mask"] & 1:
+                L["mask"] >>= 1
+                L["next"] += 1
+            prog[l] = L["next"] if L["next"] < hi else 1 << 30
+            room = max(cons, lo) + RX_R - RX_CB
+            for d in range(RX_D):
+                if L["sd"][d] is None and L["assign"] < hi and L["assign"] < room and L["assign"] - L["next"] < 32:
+                    L["sd"][d] = L["assign"]
+                    L["issued"][d] = tick
+                    L["assign"] += 1
+        # compute: step st runs once the gate has seen every active lane's input of st
+        if all(rng is None or not (rng[0] <= st < rng[1]) or prog[l] > st for l, rng in enumerate(lanes)):
+            for l, rng in enumerate(lanes):
+                if rng is not None and rng[0] <= st < rng[1]:
+                    assert ring[st % RX_R][l] == st, (l, st, ring[st % RX_R].get(l))
+            if ((st + 1) % RX_CB) == 0:
+                cons = st                                  # steps below st have been read
+            st += 1
+    return tick
+
+
+@pytest.mark.parametrize("bwd", [False, True])
+def test_receiver_ring_and_gate(bwd):
+    for nx, seed in itertools.product((1, 5, 40, 100, 256), range(4)):
+        s_planes = nx + SBJ + SBK - 2
+        lanes = []
+        for lane in range(32):
+            e, idx = lane >> 4, lane & 15
+            jl, kl = (SBJ - 1 if bwd else 0, idx) if e == 0 else (idx, SBK - 1 if bwd else 0)
+            if (lane * 7 + seed) % 9 == 0:
+                lanes.append(None)                         # no producer on this edge pencil
+                continue
+            lo = s_planes - nx - jl - kl if bwd else jl + kl
+            lanes.append((lo, lo + nx))
+        ticks = rx_emulate(s_planes, lanes, seed)
+        assert ticks >= s_planes
