@@ -20,6 +20,8 @@ roofline   the dominant kernel class: algorithmic bytes per launch / average
            stream around every launch of a second timed pass of the same K steps
            (the headline pass runs without them), against MEASURED_PEAKS.json's
            HBM copy bandwidth.
+kernel_rooflines  the same for every kernel class with a per-unit byte count (sweeps,
+           CG vector kernels, G2P), and the G2P pass against the nominal FP32 rate.
 cpu_baseline  the oracle (C restatement of the reference's CPU path, single
            thread like the reference) timed on a bounded sample of this workload
            and scaled to one substep.
@@ -81,11 +83,17 @@ BYTES = {
 }
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# FP32 sweeps (the clustered k_tri_cl) on this exact workload, from one ncu capture
-# of the 5th/6th k_tri_cl launches of this bench's mixed run.  A sweep streams every
+# FP32 sweeps (k_tri) on this exact workload, from one single-pass ncu capture of
+# two forward / backward pairs of this bench's mixed run.  A sweep streams every
 # plane of each block that holds fluid (134 of the 256 blocks here), air and
 # padding slots included.
 TRAFFIC = {"mic0_forward": 97.1e6, "mic0_backward": 143.2e6}
+
+# FP32 work of the fused PIC/FLIP + RK4 pass per particle: 5 Catmull-Rom samples
+# (MAC at the particle and the 3 later RK4 stages, saved field at the particle) x
+# 3 components x (64 taps: 84 multiply-adds; 3 x 4 weights: ~36 flops) ~ 2,550 flops
+G2P_FLOP_PER_PARTICLE = 2550
+SM_COUNT, FP32_LANES_PER_SM = 152, 128
 
 
 def rank_info():
@@ -939,6 +947,31 @@ def main(args):
                     "bytes_per_launch": bpu * unit_count, "avg_launch_ms": avg_s * 1e3,
                     "working_launches": working, "traffic": TRAFFIC.get(dom),
                     "traffic_source": "ncu capture of this workload" if dom in TRAFFIC else None}
+        # every kernel class with a per-unit byte count, and the G2P pass against FP32 issue
+        kroof = {}
+        for cls, (ms_tot, nl) in prof.items():
+            if ms_tot <= 0:
+                continue
+            if cls in ("mic0_forward", "mic0_backward"):
+                work, units = sum(s["sweeps"] for s in st), F
+            elif cls in ("matvec", "axpy", "update_search"):
+                work, units = sum(max(s["cg_iterations"], 0) + s["refinements"] for s in st), F
+            elif cls == "g2p_advect":
+                work, units = nl, N
+            else:
+                continue
+            if work <= 0 or (cls, 1) not in BYTES:
+                continue
+            avg = ms_tot / 1e3 / work
+            gbs = BYTES[(cls, 1)] * units / avg / 1e9
+            kroof[cls] = {"avg_launch_ms": round(avg * 1e3, 4), "hbm_gbs": round(gbs, 1),
+                          "hbm_frac": round(gbs / peak, 4)}
+            if cls == "g2p_advect":
+                mhz = (mixed["clocks"] or {}).get("sm_mhz") or 2070.0
+                nominal = SM_COUNT * FP32_LANES_PER_SM * 2 * mhz * 1e6 / 1e12
+                tf = G2P_FLOP_PER_PARTICLE * units / avg / 1e12
+                kroof[cls].update({"fp32_tflops": round(tf, 2), "fp32_frac_of_nominal": round(tf / nominal, 3),
+                                   "fp32_nominal_tflops": round(nominal, 1)})
         breakdown = {k: round(v[0] / args.steps, 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0]) if v[0] > 0}
         pbreak = {k: round(v[0] / args.steps, 3) for k, v in sorted(plain["prof"].items(), key=lambda kv: -kv[1][0]) if v[0] > 0}
         plain_rate = world * args.steps / plain["t"]
@@ -984,6 +1017,7 @@ def main(args):
                      "d2h_bytes_per_step": d2h // args.steps}),
             "gpu_launches": int(mixed["launches"]),
             "roofline": roof,
+            "kernel_rooflines": kroof,
             "cpu_baseline": cpu,
             "clocks": clocks,
             "adjoint": adjoint,
