@@ -75,3 +75,47 @@ def test_noalloc_rejects_overflowing_dims_before_any_device_work(lib):
             lib.gfs_tricubic_interpolate_noalloc(*dims, 0.1, dummy, dummy, dummy, dummy, 1, dummy, None)
         assert e.value.code == _lib.GFS_ERR_INVALID
         assert "too large" in str(e.value) or "scratch" in str(e.value)
+
+
+# ---- the reference's FluidSimulation C exports (include/gfs_fluidsimulation_c.h)
+
+FSIM_HEADER = os.path.join(ROOT, "include", "gfs_fluidsimulation_c.h")
+
+
+def _fsim_declared():
+    src = open(FSIM_HEADER).read()
+    return sorted(set(re.findall(r"\b((?:FluidSimulation|CBindings)_\w+)\s*\(", src)))
+
+
+def test_fluidsimulation_exports(lib):
+    names = _fsim_declared()
+    assert "FluidSimulation_update" in names and "CBindings_get_error_message" in names
+    for name in names:
+        assert hasattr(lib, name), name
+
+
+def test_fluidsimulation_exports_host_only(lib):
+    """The reference's error convention (int *err: 1 success, 0 failure, message
+    from CBindings_get_error_message) on calls that need no GPU."""
+    c_int, c_double, c_void_p, byref = ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.byref
+    lib.CBindings_get_error_message.restype = ctypes.c_char_p
+    lib.FluidSimulation_new_from_empty.restype = c_void_p
+    lib.FluidSimulation_new_from_empty.argtypes = [c_void_p]
+    err = c_int(-1)
+    obj = lib.FluidSimulation_new_from_empty(byref(err))
+    assert err.value == 1 and obj
+    i, j, k = c_int(7), c_int(7), c_int(7)
+    lib.FluidSimulation_get_grid_dimensions.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
+    lib.FluidSimulation_get_grid_dimensions(obj, byref(i), byref(j), byref(k), byref(err))
+    assert err.value == 1 and (i.value, j.value, k.value) == (0, 0, 0)
+    # an empty simulation has no grid to step
+    lib.FluidSimulation_update.argtypes = [c_void_p, c_double, c_void_p]
+    lib.FluidSimulation_update(obj, 0.01, byref(err))
+    assert err.value == 0 and b"no grid" in lib.CBindings_get_error_message()
+    lib.FluidSimulation_destroy.argtypes = [c_void_p]
+    lib.FluidSimulation_destroy(obj)
+    # bad dimensions are refused before any device work
+    lib.FluidSimulation_new_from_dimensions.restype = c_void_p
+    lib.FluidSimulation_new_from_dimensions.argtypes = [c_int, c_int, c_int, c_double, c_void_p]
+    assert not lib.FluidSimulation_new_from_dimensions(0, 8, 8, 0.1, byref(err))
+    assert err.value == 0 and b"positive" in lib.CBindings_get_error_message()
