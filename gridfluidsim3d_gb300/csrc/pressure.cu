@@ -699,105 +699,90 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 1) k_sweep(SweepArgs<T> A) {
     }
 }
 
-// ---------------------------------------------------- receiver warp
+// ---------------------------------------------------- receiver warps
 //
 // The L2 hand-over between blocks.  A block's 32 upstream edge pencils (16 on
 // the j edge, 16 on the k edge) each need one exchange word per step from a
 // producer block.  Polled by the pencils themselves, a word that is not there
 // yet costs the whole block an L2 round trip per step; near a block's start,
 // where it runs just behind its producer, that is every step, and the polling
-// branches and fences lengthen every step of the edge warps.  Instead, one extra
-// warp per block (the receiver) keeps RX_D reads in flight per edge pencil,
-// re-reads every pending step once per round, and publishes the words in a
-// shared ring: values, then the pencil's progress (all steps below it are in the
-// ring).  Before the barrier that ends step st, warp 0 (the gate) waits until
+// branches and fences lengthen every step of the edge warps.  Instead, RX_NR
+// extra warps per block (the receivers) poll the words: lane l of receiver warp
+// r takes the steps s = r (mod RX_NR) of edge pencil l, with one read in flight
+// (several reads in flight from one thread do not overlap: each extra one added
+// about a round trip to every hand-over), and publishes each word in a shared
+// ring: value, then the class's progress (every step of the class below it is in
+// the ring).  Before the barrier that ends step st, warp 0 (the gate) waits until
 // every edge pencil's input of step st+1 is there -- in the ring, or for a
 // hand-over inside a thread-block cluster in the block's receive buffer -- so the
 // compute threads read their neighbours with plain loads, and the gate hands
 // ring slots back for all pencils together every RX_CB steps.
 static constexpr int RX_R = 32;    // ring steps per pencil
-static constexpr int RX_D = 4;     // reads in flight per pencil
+static constexpr int RX_NR = 4;    // receiver warps (step classes)
 static constexpr int RX_CB = 8;    // steps between slot hand-backs
-static constexpr int RX_THREADS = 32;
+static constexpr int RX_THREADS = 32 * RX_NR;
 static constexpr int RX_DONE = 0x7fffffff;   // progress of a pencil with nothing (more) to receive
 
 template <class T>
 struct RxRing {
     T val[RX_R][32];
-    int prog[32];   // lane l: steps below prog[l] are in val
-    int cons;       // steps below cons have been read by the compute threads
+    int prog[RX_NR][32];   // class r, lane l: the steps of class r below prog[r][l] are in val
+    int cons;              // steps below cons have been read by the compute threads
 };
 
 __device__ __forceinline__ int ld_volatile_s32(const int *p) { return *(const volatile int *)p; }
 __device__ __forceinline__ void st_volatile_s32(int *p, int v) { *(volatile int *)p = v; }
 
-// Receiver lane: steps [s_lo, s_hi) of one edge pencil, whose word of step s is
-// at src + s * xs.  A read that has not seen the tag after `limit` rounds marks
-// the timeout; either way the lane ends by publishing RX_DONE, so that the gate
-// never waits on it again.
+// Receiver lane: the steps s = cls (mod RX_NR) in [s_lo, s_hi) of one edge pencil,
+// whose word of step s is at src + s * xs.  A read that has not seen the tag after
+// `limit` rounds marks the timeout; either way the lane ends by publishing
+// RX_DONE, so that the gate never waits on it again.
 template <class T>
-__device__ void rx_receive(RxRing<T> &R, int lane, const unsigned long long *src, long long xs, int s_lo, int s_hi,
-                           unsigned tag, int limit, PsCtrl *ctrl) {
+__device__ void rx_receive(RxRing<T> &R, int cls, int lane, const unsigned long long *src, long long xs, int s_lo,
+                           int s_hi, unsigned tag, int limit, PsCtrl *ctrl) {
     using X = Xch<T>;
-    unsigned long long w[RX_D][X::W];
-    int sd[RX_D];
-    int next = s_lo, assign = s_lo;
-    unsigned mask = 0u;   // bit b: step next + b is in the ring
-    st_volatile_s32(&R.prog[lane], s_lo);
-#pragma unroll
-    for (int d = 0; d < RX_D; d++) {
-        sd[d] = -1;
-        if (assign < s_hi) {
-            sd[d] = assign;
-            X::fetch(src + (long long)assign * xs, w[d]);
-            assign++;
-        }
-    }
+    unsigned long long w[X::W];
+    int s = s_lo + ((cls - s_lo) % RX_NR + RX_NR) % RX_NR;   // the first step of the class at or after s_lo
+    st_volatile_s32(&R.prog[cls][lane], s);
+    bool inflight = false;
     int rounds = 0;
-    while (next < s_hi) {
+    while (s < s_hi) {
         if (++rounds > limit) {
             atomicOr(&ctrl->err, GFS_DEV_ERR_TIMEOUT);
             break;
         }
-#pragma unroll
-        for (int d = 0; d < RX_D; d++) {
-            if (sd[d] >= 0) {
-                if (X::ready(w[d], tag)) {
-                    R.val[sd[d] & (RX_R - 1)][lane] = X::value(w[d]);
-                    mask |= 1u << (sd[d] - next);
-                    sd[d] = -1;
-                } else {
-                    X::fetch(src + (long long)sd[d] * xs, w[d]);
-                }
+        if (!inflight) {
+            // ring slot s & (RX_R-1) is free once the compute threads have read step s - RX_R
+            if (s < max(ld_volatile_s32(&R.cons), s_lo) + RX_R - RX_CB) {
+                X::fetch(src + (long long)s * xs, w);
+                inflight = true;
+            } else {
+                __nanosleep(32);   // ahead of the compute threads: leave them the issue slots
             }
-        }
-        if (mask & 1u) {
-            while (mask & 1u) {
-                mask >>= 1;
-                next++;
+        } else if (X::ready(w, tag)) {
+            R.val[s & (RX_R - 1)][lane] = X::value(w);
+            s += RX_NR;
+            __threadfence_block();   // the value before the progress
+            st_volatile_s32(&R.prog[cls][lane], s);
+            inflight = false;
+            if (s < s_hi && s < max(ld_volatile_s32(&R.cons), s_lo) + RX_R - RX_CB) {
+                X::fetch(src + (long long)s * xs, w);
+                inflight = true;
             }
-            __threadfence_block();   // the values before the progress
-            st_volatile_s32(&R.prog[lane], next);
-        }
-        const int room = max(ld_volatile_s32(&R.cons), s_lo) + RX_R - RX_CB;
-#pragma unroll
-        for (int d = 0; d < RX_D; d++) {
-            if (sd[d] < 0 && assign < s_hi && assign < room && assign - next < 32) {
-                sd[d] = assign;
-                X::fetch(src + (long long)assign * xs, w[d]);
-                assign++;
-            }
+        } else {
+            X::fetch(src + (long long)s * xs, w);
         }
     }
     __threadfence_block();
-    st_volatile_s32(&R.prog[lane], RX_DONE);
+    st_volatile_s32(&R.prog[cls][lane], RX_DONE);
 }
 
 // Gate (warp 0, lane l for edge pencil l): wait until the input of step `need` of
-// every edge pencil is readable -- L2 pencils: the receiver's progress is past it
-// (cached in `seen`); cluster pencils: the tagged word is in the receive buffer
-// (rxw: the word of step 0, stride rxs words per step); pencils that need nothing
-// at `need` pass.  Bounded; a timeout marks the error and lets every later gate pass.
+// every edge pencil is readable -- L2 pencils: every class's progress is past it
+// (their minimum cached in `seen`); cluster pencils: the tagged word is in the
+// receive buffer (rxw: the word of step 0, stride rxs words per step); pencils that
+// need nothing at `need` pass.  Bounded; a timeout marks the error and lets every
+// later gate pass.
 template <class T>
 __device__ __forceinline__ void rx_gate(RxRing<T> &R, int lane, int need, bool l2, bool cl, int lo, int hi,
                                         const unsigned long long *rxw, long long rxs, unsigned tag, int &seen,
@@ -809,7 +794,10 @@ __device__ __forceinline__ void rx_gate(RxRing<T> &R, int lane, int need, bool l
         bool ok = true;
         if (wants && !timed_out) {
             if (l2 && need >= seen) {
-                seen = ld_volatile_s32(&R.prog[lane]);
+                int m = ld_volatile_s32(&R.prog[0][lane]);
+#pragma unroll
+                for (int r = 1; r < RX_NR; r++) m = min(m, ld_volatile_s32(&R.prog[r][lane]));
+                seen = m;
                 ok = need < seen;
             } else if (cl) {
                 unsigned long long w[X::W];
@@ -858,7 +846,7 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
         sh_ticket = atomicAdd(A.ticket, 1u);
         sh_epoch = A.ctrl->epoch;
     }
-    if (tid < 32) rxr.prog[tid] = 0;
+    for (int q = tid; q < RX_NR * 32; q += blockDim.x) (&rxr.prog[0][0])[q] = 0;
     if (tid == 0) rxr.cons = 0;
     __syncthreads();
     const unsigned t = sh_ticket, tag = sh_epoch;
@@ -881,8 +869,8 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
     Acc2f dot32;
     double dot64 = 0.0;
     if (tid >= SPLANE) {
-        // receiver warp: lane l < 16 feeds the j-edge pencil kl = l, lane 16 + l the k-edge pencil jl = l
-        const int lane = tid - SPLANE, e = lane >> 4, idx = lane & 15;
+        // receiver warps (class cls): lane l < 16 feeds the j-edge pencil kl = l, lane 16 + l the k-edge pencil jl = l
+        const int cls = (tid - SPLANE) >> 5, lane = (tid - SPLANE) & 31, e = lane >> 4, idx = lane & 15;
         const int jl_c = e == 0 ? (bwd ? SBJ - 1 : 0) : idx, kl_c = e == 0 ? idx : (bwd ? SBK - 1 : 0);
         const bool valid_c = live && bj * SBJ + jl_c < K.ny && bk * SBK + kl_c < K.nz;
         if (valid_c && (e == 0 ? has_pj : has_pk)) {
@@ -893,7 +881,7 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
                        : A.xch + (long long)(pbk * K.nbj + bj) * xblock +
                              (bwd ? (long long)(S - 1 - (SBK - 1)) : (long long)(SBK - 1)) * XP +
                              (long long)(SBJ + idx) * X::W;
-            rx_receive<T>(rxr, lane, src, XS, lo, lo + K.nx, wtag, A.spin_limit, A.ctrl);
+            rx_receive<T>(rxr, cls, lane, src, XS, lo, lo + K.nx, wtag, A.spin_limit, A.ctrl);
         }
     } else {
     const int jl = tid % SBJ, kl = tid / SBJ;
@@ -1028,7 +1016,7 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
     __threadfence();
     if (MODE == SW_BWD) {
         double acc = 0.0;
-        for (unsigned q = tid; q < nblocks; q += SPLANE) acc += __ldcg(A.partials + q);
+        for (unsigned q = tid; q < nblocks; q += blockDim.x) acc += __ldcg(A.partials + q);
         acc = block_reduce<0>(acc);
         if (tid == 0) {
             PsCtrl *C = A.ctrl;
@@ -1117,7 +1105,7 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE + R
     const int NR = rx_steps(S);
     unsigned long long *rxj = rx, *rxk = rx + (long long)NR * SBK * W;
     for (int q = tid; q < 2 * NR * SBK * W; q += blockDim.x) rx[q] = 0ull;
-    if (tid < 32) rxr.prog[tid] = 0;
+    for (int q = tid; q < RX_NR * 32; q += blockDim.x) (&rxr.prog[0][0])[q] = 0;
     if (tid == 0) rxr.cons = 0;
     if (tid == 0) {
         if (rank == 0) sh_ticket = atomicAdd(A.ticket, 1u);
@@ -1150,9 +1138,9 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE + R
     Acc2f dot32;
     double dot64 = 0.0;
     if (tid >= SPLANE) {
-        // receiver warp for the edges fed through L2: lane l < 16 feeds the j-edge
-        // pencil kl = l, lane 16 + l the k-edge pencil jl = l
-        const int lane = tid - SPLANE, e = lane >> 4, idx = lane & 15;
+        // receiver warps (class cls) for the edges fed through L2: lane l < 16 feeds
+        // the j-edge pencil kl = l, lane 16 + l the k-edge pencil jl = l
+        const int cls = (tid - SPLANE) >> 5, lane = (tid - SPLANE) & 31, e = lane >> 4, idx = lane & 15;
         const int jl_c = e == 0 ? (bwd ? SBJ - 1 : 0) : idx, kl_c = e == 0 ? idx : (bwd ? SBK - 1 : 0);
         const bool valid_c = live && bj * SBJ + jl_c < K.ny && bk * SBK + kl_c < K.nz;
         if (valid_c && (e == 0 ? has_pj && !pj_cl : has_pk && !pk_cl)) {
@@ -1163,7 +1151,7 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE + R
                        : A.xch + (long long)(pbk * K.nbj + bj) * xblock +
                              (bwd ? (long long)(S - 1 - (SBK - 1)) : (long long)(SBK - 1)) * XP +
                              (long long)(SBJ + idx) * W;
-            rx_receive<T>(rxr, lane, src, XS, lo, lo + K.nx, wtag, A.spin_limit, A.ctrl);
+            rx_receive<T>(rxr, cls, lane, src, XS, lo, lo + K.nx, wtag, A.spin_limit, A.ctrl);
         }
     } else {
     const int jl = tid % SBJ, kl = tid / SBJ;
@@ -1316,7 +1304,7 @@ __global__ void __cluster_dims__(CL_J * CL_K, 1, 1) __launch_bounds__(SPLANE + R
     if (MODE == SW_BWD) {
         const unsigned nblocks = (unsigned)(K.nbj * K.nbk);
         double acc = 0.0;
-        for (unsigned q = tid; q < nblocks; q += SPLANE) acc += __ldcg(A.partials + q);
+        for (unsigned q = tid; q < nblocks; q += blockDim.x) acc += __ldcg(A.partials + q);
         acc = block_reduce<0>(acc);
         if (tid == 0) {
             PsCtrl *C = A.ctrl;

@@ -451,8 +451,8 @@ int gfs_ctx_launch_count(gfs_ctx *ctx, int64_t *count);
 /* The MIC(0) triangular solves (PressureSolver::_applyPreconditioner,
    pressuresolver.cpp:304-386) run as i+j+k hyperplane wavefronts over blocks
    of 16 x 16 pencils.  Three kernels compute the same values in the same order:
-   BLOCK hands block-edge values over through L2 words (one receiver warp per
-   block polls them into shared memory); CLUSTER_4X2 / _2X2 group 4 x 2 or 2 x 2
+   BLOCK hands block-edge values over through L2 words (four receiver warps per
+   block poll them into shared memory); CLUSTER_4X2 / _2X2 group 4 x 2 or 2 x 2
    blocks into a thread-block cluster whose blocks hand over through distributed
    shared memory.  AUTO (the default) runs BLOCK, the fastest of the three on
    GB300 at 128^3 and 256^3.

@@ -146,19 +146,21 @@ def test_ring_refill_order(p):
 
 
 # ----------------------------------------------------------------------------
-# The receiver warp and the gate (csrc/pressure.cu rx_receive, rx_gate, k_tri):
-# a discrete-time restatement with random producer and load timing.  Each tick
-# every receiver lane runs one round (completed loads that see the step's word
-# publish it into ring slot step % RX_R, the others are reissued, progress is
-# published, free load slots take the next steps within room = max(cons, lo) +
-# RX_R - RX_CB); the compute threads run step st once the gate has seen every
-# lane's progress past st (for lanes active at st), read ring slot st % RX_R, and
-# every RX_CB steps hand back the slots below st.  Checked: no slot is written
-# while it holds a step not yet read, every read finds its own step's value, and
-# the sweep ends within a bounded number of ticks (no circular wait), for lanes
-# with different active ranges (forward and backward) and lanes without a producer.
+# The receiver warps and the gate (csrc/pressure.cu rx_receive, rx_gate, k_tri):
+# a discrete-time restatement with random producer and load timing.  Lane l of
+# receiver class r takes the steps s = r (mod RX_NR) of edge pencil l with one read
+# in flight: each tick it issues the read of its next step if that step is within
+# room = max(cons, lo) + RX_R - RX_CB, or, once its read has seen the word,
+# publishes it into ring slot s % RX_R and moves on by RX_NR, or reissues the read.
+# The compute threads run step st once the gate has seen, for every lane active at
+# st, the minimum progress over the classes past st; they read ring slot st % RX_R
+# and every RX_CB steps hand back the slots below st.  Checked: no slot is written
+# while it holds a step not yet read, every read finds its own step's value, and the
+# sweep ends within a bounded number of ticks (no circular wait), for lanes with
+# different active ranges (forward and backward) and lanes without a producer.
 
-RX_R, RX_D, RX_CB = 32, 4, 8
+RX_R, RX_NR, RX_CB = 32, 4, 8
+DONE = 1 << 30
 
 
 def rx_emulate(s_planes, lanes, seed):
@@ -176,52 +178,52 @@ def rx_emulate(s_planes, lanes, seed):
                 a[s] = t
         avail.append(a)
     ring = {}                   # slot -> (lane -> step it holds)
-    prog = [0] * len(lanes)
+    prog = [[0] * RX_NR for _ in lanes]
     cons = 0
-    st_lanes = []
+    cl = []                     # per lane, per class: [next step, read in flight, tick it was issued]
     for l, rng in enumerate(lanes):
         if rng is None:
-            st_lanes.append(None)
+            cl.append(None)
             continue
         lo, hi = rng
-        st_lanes.append({"next": lo, "assign": lo, "mask": 0, "sd": [None] * RX_D, "issued": [0] * RX_D})
-        prog[l] = lo
+        row = []
+        for r in range(RX_NR):
+            s0 = lo + (r - lo) % RX_NR
+            row.append([s0, False, 0])
+            prog[l][r] = s0 if s0 < hi else DONE
+        cl.append(row)
     tick, st = 0, 0
     limit = 50 * (s_planes + 100)
     while st < s_planes:
         tick += 1
         assert tick < limit, "the sweep did not finish: a wait that never ends"
-        # receiver lanes: one round each
         for l, rng in enumerate(lanes):
-            L = st_lanes[l]
-            if L is None or L["next"] >= rng[1]:
+            if cl[l] is None:
                 continue
             lo, hi = rng
-            for d in range(RX_D):
-                s = L["sd"][d]
-                if s is None:
+            room = max(cons, lo) + RX_R - RX_CB
+            for r in range(RX_NR):
+                c = cl[l][r]
+                s = c[0]
+                if s >= hi:
                     continue
-                if avail[l][s] <= L["issued"][d]:          # the load saw the word
+                if not c[1]:
+                    if s < room:
+                        c[1], c[2] = True, tick
+                elif avail[l][s] <= c[2]:                  # the read saw the word
                     slot = s % RX_R
                     held = ring.setdefault(slot, {}).get(l)
                     assert held is None or held < cons, (l, s, held, cons)   # its step was read
                     ring[slot][l] = s
-                    L["mask"] |= 1 << (s - L["next"])
-                    L["sd"][d] = None
+                    s += RX_NR
+                    c[0], c[1] = s, False
+                    prog[l][r] = s if s < hi else DONE
+                    if s < hi and s < room:
+                        c[1], c[2] = True, tick
                 else:
-                    L["issued"][d] = tick                  # reissue
-            while L["mask"] & 1:
-                L["mask"] >>= 1
-                L["next"] += 1
-            prog[l] = L["next"] if L["next"] < hi else 1 << 30
-            room = max(cons, lo) + RX_R - RX_CB
-            for d in range(RX_D):
-                if L["sd"][d] is None and L["assign"] < hi and L["assign"] < room and L["assign"] - L["next"] < 32:
-                    L["sd"][d] = L["assign"]
-                    L["issued"][d] = tick
-                    L["assign"] += 1
+                    c[2] = tick                            # reissue
         # compute: step st runs once the gate has seen every active lane's input of st
-        if all(rng is None or not (rng[0] <= st < rng[1]) or prog[l] > st for l, rng in enumerate(lanes)):
+        if all(rng is None or not (rng[0] <= st < rng[1]) or min(prog[l]) > st for l, rng in enumerate(lanes)):
             for l, rng in enumerate(lanes):
                 if rng is not None and rng[0] <= st < rng[1]:
                     assert ring[st % RX_R][l] == st, (l, st, ring[st % RX_R].get(l))
