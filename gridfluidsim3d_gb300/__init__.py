@@ -7,7 +7,7 @@ package is its host-side mirror; importing it needs no GPU, calling into it
 does, and there is no CPU fallback.
 """
 from ._lib import GFSError, PRECISION_MIXED, PRECISION_PLAIN  # noqa: F401
-from ._lib import (SWEEP_AUTO, SWEEP_BLOCK, SWEEP_CLUSTER_2X2, SWEEP_CLUSTER_4X2,  # noqa: F401
+from ._lib import (SWEEP_AUTO, SWEEP_BLOCK, SWEEP_CLUSTER_2X2, SWEEP_CLUSTER_4X2, SWEEP_WARP,  # noqa: F401
                    STAGE_ALL, STAGE_APPLY_PRESSURE, STAGE_BODY_FORCES, STAGE_EXTRAPOLATE, STAGE_PRESSURE,
                    STAGE_UPDATE_FLUID_CELLS)
 from . import config  # noqa: F401

@@ -28,6 +28,7 @@ SWEEP_AUTO = 0
 SWEEP_BLOCK = 1
 SWEEP_CLUSTER_4X2 = 2
 SWEEP_CLUSTER_2X2 = 3
+SWEEP_WARP = 4
 STAGE_UPDATE_FLUID_CELLS = 1
 STAGE_BODY_FORCES = 6
 STAGE_PRESSURE = 7

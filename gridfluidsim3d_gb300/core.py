@@ -151,7 +151,7 @@ class Context:
 
     # -- wavefront kernels of the MIC(0) triangular solves (gfs_ctx_set_sweep_kernel) --
     def set_sweep_kernel(self, kind: int):
-        """SWEEP_AUTO (default), SWEEP_BLOCK, SWEEP_CLUSTER_4X2 or SWEEP_CLUSTER_2X2."""
+        """SWEEP_AUTO (default), SWEEP_BLOCK, SWEEP_CLUSTER_4X2, SWEEP_CLUSTER_2X2 or SWEEP_WARP (FP32 solves)."""
         _lib.lib().gfs_ctx_set_sweep_kernel(self._h, int(kind))
 
     def last_sweep_kernel(self) -> int:

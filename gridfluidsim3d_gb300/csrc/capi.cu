@@ -508,8 +508,8 @@ int gfs_ctx_launch_count(gfs_ctx *ctx, int64_t *count) {
 
 int gfs_ctx_set_sweep_kernel(gfs_ctx *ctx, int kind) {
     GFS_NONNULL(ctx);
-    if (kind < GFS_SWEEP_AUTO || kind > GFS_SWEEP_CLUSTER_2X2) {
-        set_error(GFS_ERR_INVALID, "sweep kernel %d is not one of GFS_SWEEP_AUTO .. GFS_SWEEP_CLUSTER_2X2", kind);
+    if (kind < GFS_SWEEP_AUTO || kind > GFS_SWEEP_WARP) {
+        set_error(GFS_ERR_INVALID, "sweep kernel %d is not one of GFS_SWEEP_AUTO .. GFS_SWEEP_WARP", kind);
         return GFS_ERR_INVALID;
     }
     ctx->c.sweep_kernel = kind;

@@ -1332,6 +1332,421 @@ template <class T>
 static size_t tri_cl_smem(int S) {
     return (size_t)2 * rx_steps(S) * SBJ * Xch<T>::W * sizeof(unsigned long long);
 }
+// ------------------------------------------------- one-warp triangular solve
+//
+// k_tri_warp (FP32 FWD / BWD): the triangular solves with ONE compute warp per
+// 16 x 16 pencil block and no per-plane barrier.  Lane L (a = L & 3, b = L >> 2)
+// owns the pencils jl' = 4a..4a+3 of the rows kl' = b and kl' = b + 8, where the
+// primed coordinates are the block's own for the forward solve and mirrored
+// (jl' = 15 - jl, kl' = 15 - kl) for the backward one, so that both walk the
+// same upstream direction: a lane's two rows are the 16-byte plane chunks L and
+// L + 32 (forward) or 63 - L and 31 - L with the four pencils reversed
+// (backward), one conflict-free 16-byte shared-memory read per row and array.
+// Per step, the i neighbour is the lane's own previous value, the j neighbour
+// the previous pencil of the row (a shuffle across the lane's left boundary),
+// the k neighbour the row below (a shuffle), and the block edges the receiver
+// ring.  The plane inputs arrive by bulk copies (cp.async.bulk, WT_G planes per
+// copy and array, WT_NG copies in flight, full / empty mbarriers) issued by one
+// loader lane; the edge words by the RX_NR receiver warps (one read in flight per
+// lane, classes of steps mod RX_NR), each publishing the step below which every
+// edge word of its class is in the ring.  Slots of cells outside the grid hold 0
+// in the input and preconditioner vectors, so such a cell computes +-0 without a
+// select and hands over +-0.  Arithmetic per cell is k_tri's; the backward
+// solve's dot(z, r) sums each lane's eight products per step before its
+// compensated running sum (deterministic; its rounding differs from k_tri's).
+static constexpr int WT_G = 8;                             // planes per bulk copy
+static constexpr int WT_NG = 4;                            // copies in flight
+static constexpr int WT_THREADS = 32 + RX_THREADS + 32;    // compute warp, receiver warps, loader warp
+static_assert(RX_CB == WT_G, "receive-ring slots are handed back once per copy group");
+
+struct WtRx {
+    float val[RX_R][32];   // step s, lane l: the edge word (l < 16: j edge of kl = l; 16 + l: k edge of jl = l)
+    int prog[RX_NR];       // class r: every edge word of the class's steps below prog[r] is in val
+    int cons;              // steps below cons have been read by the compute warp
+};
+
+template <int MODE>
+static constexpr size_t tri_warp_smem() {
+    return (size_t)WT_NG * (MODE == SW_BWD ? 3 : 2) * WT_G * SPLANE * sizeof(float) +
+           2 * WT_NG * sizeof(unsigned long long);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *mb, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mb)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *mb, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mb)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long *mb) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(mb)) : "memory");
+}
+// potentially blocking test of the phase with the given parity (the thread may be
+// suspended for a bounded time); true once that phase has completed
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *mb, unsigned parity) {
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok)
+                 : "r"(smem_addr(mb)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+// bulk copy global -> shared (16-byte aligned addresses, size a multiple of 16),
+// completing bytes on the mbarrier
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *mb) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(mb))
+                 : "memory");
+}
+// tagged exchange words without a branch: stored only where pred is nonzero
+__device__ __forceinline__ void put_word(unsigned long long *p, float v, unsigned tag, unsigned pred) {
+    const unsigned long long w = ((unsigned long long)tag << 32) | (unsigned long long)__float_as_uint(v);
+    asm volatile("{\n .reg .pred q;\n setp.ne.u32 q, %2, 0;\n @q st.relaxed.gpu.global.u64 [%0], %1;\n}\n"
+                 ::"l"(p), "l"(w), "r"(pred)
+                 : "memory");
+}
+__device__ __forceinline__ void put_words2(unsigned long long *p, float v0, float v1, unsigned tag, unsigned pred) {
+    const unsigned long long w0 = ((unsigned long long)tag << 32) | (unsigned long long)__float_as_uint(v0);
+    const unsigned long long w1 = ((unsigned long long)tag << 32) | (unsigned long long)__float_as_uint(v1);
+    asm volatile("{\n .reg .pred q;\n setp.ne.u32 q, %3, 0;\n @q st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};\n}\n"
+                 ::"l"(p), "l"(w0), "l"(w1), "r"(pred)
+                 : "memory");
+}
+// the four floats of a 16-byte chunk in pencil order (reversed for the mirrored backward solve)
+template <bool REV>
+__device__ __forceinline__ void unpack4(const float4 v, float o[4]) {
+    if (REV) { o[0] = v.w; o[1] = v.z; o[2] = v.y; o[3] = v.x; }
+    else { o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w; }
+}
+template <bool REV>
+__device__ __forceinline__ float4 pack4(const float o[4]) {
+    return REV ? make_float4(o[3], o[2], o[1], o[0]) : make_float4(o[0], o[1], o[2], o[3]);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(WT_THREADS, 1) k_tri_warp(SweepArgs<float> A) {
+    using Op = Ar<float>;
+    static_assert(MODE == SW_FWD || MODE == SW_BWD, "triangular solves only");
+    constexpr bool bwd = MODE == SW_BWD;
+    constexpr int NARR = bwd ? 3 : 2;
+    constexpr unsigned FULL = 0xffffffffu;
+    constexpr long long XP = XCH_PER_PLANE;   // words per block plane (one per FP32 entry)
+    constexpr long long XS = bwd ? -XP : XP;
+    constexpr long long PS = bwd ? -(long long)SPLANE : (long long)SPLANE;
+    extern __shared__ __align__(128) unsigned char wt_smem[];
+    float (*ring)[NARR][WT_G][SPLANE] = reinterpret_cast<float (*)[NARR][WT_G][SPLANE]>(wt_smem);
+    unsigned long long *mfull =
+        reinterpret_cast<unsigned long long *>(wt_smem + (size_t)WT_NG * NARR * WT_G * SPLANE * sizeof(float));
+    unsigned long long *mempty = mfull + WT_NG;
+    __shared__ __align__(16) WtRx rx;
+    __shared__ unsigned sh_ticket, sh_epoch;
+    if (A.ctrl->done) return;   // the same value in every block of the launch
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const Skew &K = A.K;
+    const int S = K.S;
+    if (tid == 0) {
+        sh_ticket = atomicAdd(A.ticket, 1u);
+        sh_epoch = A.ctrl->epoch;
+        rx.cons = 0;
+    }
+    if (tid < RX_NR) rx.prog[tid] = 0;
+    for (int q = tid; q < RX_R * 32; q += WT_THREADS) (&rx.val[0][0])[q] = 0.f;
+    if (tid == WT_THREADS - 32) {
+        for (int u = 0; u < WT_NG; u++) {
+            mbar_init(&mfull[u], 1);
+            mbar_init(&mempty[u], 1);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    const unsigned t = sh_ticket, tag = sh_epoch;
+    const unsigned wtag = tag + A.wait_skew;   // the tag the waits look for (tag itself unless a test skews it)
+    int bj = (int)(t % K.nbj), bk = (int)(t / K.nbj);
+    if (bwd) {
+        bj = K.nbj - 1 - bj;
+        bk = K.nbk - 1 - bk;
+    }
+    const int pbj = bwd ? bj + 1 : bj - 1, pbk = bwd ? bk + 1 : bk - 1;
+    const int cbj = bwd ? bj - 1 : bj + 1, cbk = bwd ? bk - 1 : bk + 1;
+    // blocks without fluid are skipped; their consumers take 0 (as k_tri)
+    const bool live = A.blkf[bk * K.nbj + bj] != 0;
+    const bool has_pj = pbj >= 0 && pbj < K.nbj && A.blkf[bk * K.nbj + pbj],
+               has_pk = pbk >= 0 && pbk < K.nbk && A.blkf[pbk * K.nbj + bj];
+    const bool has_cj = cbj >= 0 && cbj < K.nbj && A.blkf[bk * K.nbj + cbj],
+               has_ck = cbk >= 0 && cbk < K.nbk && A.blkf[cbk * K.nbj + bj];
+    const long long xblock = (long long)S * XP;
+    const long long base = K.base(bj, bk);
+    const int ngroups = live ? (S + WT_G - 1) / WT_G : 0;
+    Acc2f dot32;
+    if (warp == WT_THREADS / 32 - 1) {
+        // loader: copy group g (steps g*G .. g*G+np-1) into slot g % WT_NG once the compute warp released it
+        if (lane == 0 && ngroups > 0) {
+            int g = 0;
+            bool to = false;
+            for (; g < ngroups; g++) {
+                const int slot = g % WT_NG;
+                if (g >= WT_NG) {
+                    int k = 0;
+                    while (!mbar_try_wait(&mempty[slot], (unsigned)((g / WT_NG - 1) & 1))) {
+                        if (++k > A.spin_limit) {
+                            atomicOr(&A.ctrl->err, GFS_DEV_ERR_TIMEOUT);
+                            to = true;
+                            break;
+                        }
+                    }
+                    if (to) break;
+                }
+                const int np = min(WT_G, S - g * WT_G);
+                // forward: planes g*G ..; backward: planes S-g*G-np .. S-1-g*G, step u at np-1-u
+                const long long p0 = base + (long long)(bwd ? S - g * WT_G - np : g * WT_G) * SPLANE;
+                const unsigned bytes = (unsigned)(np * SPLANE * sizeof(float));
+                mbar_arrive_expect_tx(&mfull[slot], (unsigned)NARR * bytes);
+                bulk_copy_g2s(&ring[slot][0][0][0], A.in + p0, bytes, &mfull[slot]);
+                bulk_copy_g2s(&ring[slot][1][0][0], A.precon + p0, bytes, &mfull[slot]);
+                if (bwd) bulk_copy_g2s(&ring[slot][NARR - 1][0][0], A.rdot + p0, bytes, &mfull[slot]);
+            }
+            // copies still in flight land before the block may exit
+            for (int q = max(0, g - WT_NG); q < g; q++) {
+                int k = 0;
+                while (!mbar_try_wait(&mfull[q % WT_NG], (unsigned)((q / WT_NG) & 1)) && ++k < A.spin_limit) {
+                }
+            }
+        }
+    } else if (warp >= 1) {
+        // receiver warp of class r: lane l < 16 the j-edge pencil kl = l, lane 16 + l the
+        // k-edge pencil jl = l; its steps s = r (mod RX_NR), one read in flight
+        const int r = warp - 1, e = lane >> 4, idx = lane & 15;
+        const int jl_c = e == 0 ? (bwd ? SBJ - 1 : 0) : idx, kl_c = e == 0 ? idx : (bwd ? SBK - 1 : 0);
+        const bool valid_c = live && bj * SBJ + jl_c < K.ny && bk * SBK + kl_c < K.nz;
+        const bool act = valid_c && (e == 0 ? has_pj : has_pk);
+        const int lo = bwd ? S - K.nx - jl_c - kl_c : jl_c + kl_c;
+        const int end = act ? lo + K.nx : 0;
+        const unsigned long long *src =
+            !act ? A.xch
+            : e == 0 ? A.xch + (long long)(bk * K.nbj + pbj) * xblock +
+                           (bwd ? (long long)(S - 1 - (SBJ - 1)) : (long long)(SBJ - 1)) * XP + idx
+                     : A.xch + (long long)(pbk * K.nbj + bj) * xblock +
+                           (bwd ? (long long)(S - 1 - (SBK - 1)) : (long long)(SBK - 1)) * XP + SBJ + idx;
+        int s = lo + ((r - lo) % RX_NR + RX_NR) % RX_NR;   // the first step of the class at or after lo
+        bool inflight = false;
+        unsigned long long w = 0ull;
+        int pub = 0, rounds = 0;
+        while (__any_sync(FULL, s < end)) {
+            if (++rounds > A.spin_limit) {
+                if (lane == 0) atomicOr(&A.ctrl->err, GFS_DEV_ERR_TIMEOUT);
+                break;
+            }
+            if (s < end) {
+                if (!inflight) {
+                    // ring slot s & (RX_R-1) is free once the compute warp has read step s - RX_R
+                    if (s < max(ld_volatile_s32(&rx.cons), lo) + RX_R - RX_CB) {
+                        w = ld_cg_u64(src + (long long)s * XS);
+                        inflight = true;
+                    } else {
+                        __nanosleep(32);
+                    }
+                } else if ((unsigned)(w >> 32) == wtag) {
+                    rx.val[s & (RX_R - 1)][lane] = __uint_as_float((unsigned)(w & 0xFFFFFFFFull));
+                    s += RX_NR;
+                    inflight = false;
+                    if (s < end && s < max(ld_volatile_s32(&rx.cons), lo) + RX_R - RX_CB) {
+                        w = ld_cg_u64(src + (long long)s * XS);
+                        inflight = true;
+                    }
+                } else {
+                    w = ld_cg_u64(src + (long long)s * XS);
+                }
+            }
+            const int m = __reduce_min_sync(FULL, s < end ? s : S);
+            if (m > pub) {
+                __syncwarp();
+                if (lane == 0) {
+                    __threadfence_block();   // the values before the progress
+                    st_volatile_s32(&rx.prog[r], m);
+                }
+                pub = m;
+            }
+        }
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            st_volatile_s32(&rx.prog[r], S);   // nothing more (or given up): no step waits on this class
+        }
+    } else if (ngroups > 0) {
+        // the compute warp
+        const int a = lane & 3, b = lane >> 2;
+        const int c0 = bwd ? 63 - lane : lane, c1 = bwd ? 31 - lane : lane + 32;   // 16-byte chunks of rows 0, 1
+        float px[2][4];
+#pragma unroll
+        for (int r = 0; r < 2; r++)
+#pragma unroll
+            for (int p = 0; p < 4; p++) px[r][p] = 0.f;
+        float *po = A.out + base + (bwd ? (long long)(S - 1) * SPLANE : 0);
+        unsigned long long *pxo = A.xch + (long long)(bk * K.nbj + bj) * xblock + (bwd ? (long long)(S - 1) * XP : 0);
+        // hand-overs: j edge (jl' = 15: a == 3, pencil 3) of rows kl' = b, b + 8 at words kl;
+        // k edge (kl' = 15: b == 7, row 1) of pencils jl' = 4a + p at words 16 + jl
+        const int wj0 = bwd ? 15 - b : b, wj1 = bwd ? 7 - b : b + 8;
+        const int wk = bwd ? 28 - 4 * a : 16 + 4 * a;
+        const unsigned out_j = a == 3 && has_cj, out_k = b == 7 && has_ck;
+        // edge inputs: j edge (jl' = 0: a == 0) of rows r at ring words wj0 / wj1; k edge
+        // (kl' = 0: b == 0, row 0) of pencils jl' = 4a + p in the 16-byte chunk at ring word ek0
+        const int ek0 = wk;
+        const float ns = A.negscale;
+        int seen = 0;
+        bool to = false;
+        for (int g = 0; g < ngroups && !to; g++) {
+            const int slot = g % WT_NG;
+            {
+                int k = 0;
+                while (!mbar_try_wait(&mfull[slot], (unsigned)((g / WT_NG) & 1))) {
+                    if (++k > A.spin_limit) {
+                        if (lane == 0) atomicOr(&A.ctrl->err, GFS_DEV_ERR_TIMEOUT);
+                        to = true;
+                        break;
+                    }
+                }
+                if (to) break;
+            }
+            const int np = min(WT_G, S - g * WT_G);
+            auto step = [&](const int u) {
+                const int st = g * WT_G + u;
+                const int ui = bwd ? np - 1 - u : u;
+                if (st >= seen) {
+                    int k = 0;
+                    for (;;) {
+                        int m = ld_volatile_s32(&rx.prog[0]);
+#pragma unroll
+                        for (int r = 1; r < RX_NR; r++) m = min(m, ld_volatile_s32(&rx.prog[r]));
+                        seen = m;
+                        if (seen > st) break;
+                        if (++k > A.spin_limit) {
+                            if (lane == 0) atomicOr(&A.ctrl->err, GFS_DEV_ERR_TIMEOUT);
+                            seen = S;
+                            break;
+                        }
+                    }
+                    __threadfence_block();   // the ring values after the progress that covers them
+                }
+                float ra[2][4], pc[2][4], rv[2][4], ek[4];
+                unpack4<bwd>(*reinterpret_cast<const float4 *>(&ring[slot][0][ui][4 * c0]), ra[0]);
+                unpack4<bwd>(*reinterpret_cast<const float4 *>(&ring[slot][0][ui][4 * c1]), ra[1]);
+                unpack4<bwd>(*reinterpret_cast<const float4 *>(&ring[slot][1][ui][4 * c0]), pc[0]);
+                unpack4<bwd>(*reinterpret_cast<const float4 *>(&ring[slot][1][ui][4 * c1]), pc[1]);
+                if (bwd) {
+                    unpack4<bwd>(*reinterpret_cast<const float4 *>(&ring[slot][NARR - 1][ui][4 * c0]), rv[0]);
+                    unpack4<bwd>(*reinterpret_cast<const float4 *>(&ring[slot][NARR - 1][ui][4 * c1]), rv[1]);
+                }
+                const float *xr = &rx.val[st & (RX_R - 1)][0];
+                const float ej[2] = {xr[wj0], xr[wj1]};
+                unpack4<bwd>(*reinterpret_cast<const float4 *>(xr + ek0), ek);
+                float nj[2][4], nk[2][4];
+#pragma unroll
+                for (int r = 0; r < 2; r++) {
+                    const float sj = __shfl_up_sync(FULL, px[r][3], 1, 4);
+                    nj[r][0] = a ? sj : ej[r];
+#pragma unroll
+                    for (int p = 1; p < 4; p++) nj[r][p] = px[r][p - 1];
+                }
+#pragma unroll
+                for (int p = 0; p < 4; p++) {
+                    const float up0 = __shfl_up_sync(FULL, px[0][p], 4);
+                    nk[0][p] = b ? up0 : ek[p];
+                    const float send = b == 7 ? px[0][p] : px[1][p];   // row 1's lower row: lane - 4's row 1, or row 0 of b = 7
+                    nk[1][p] = __shfl_sync(FULL, send, (lane - 4) & 31);
+                }
+                float val[2][4];
+                float part = 0.f;
+#pragma unroll
+                for (int r = 0; r < 2; r++)
+#pragma unroll
+                    for (int p = 0; p < 4; p++) {
+                        if (!bwd) {
+                            // _applyPreconditioner forward solve (pressuresolver.cpp:311-351), as k_tri
+                            val[r][p] = Op::mul(Op::sub(Op::sub(Op::sub(ra[r][p], px[r][p]), nj[r][p]), nk[r][p]), pc[r][p]);
+                            px[r][p] = Op::mul(Op::mul(ns, pc[r][p]), val[r][p]);
+                        } else {
+                            // backward solve (pressuresolver.cpp:354-385), as k_tri
+                            const float m = Op::mul(ns, pc[r][p]);
+                            val[r][p] = Op::mul(Op::sub(Op::sub(Op::sub(ra[r][p], Op::mul(m, px[r][p])), Op::mul(m, nj[r][p])),
+                                                        Op::mul(m, nk[r][p])),
+                                                pc[r][p]);
+                            px[r][p] = val[r][p];
+                            part = fmaf(val[r][p], rv[r][p], part);
+                        }
+                    }
+                if (bwd) dot32.add(part);
+                *reinterpret_cast<float4 *>(po + 4 * c0) = pack4<bwd>(val[0]);
+                *reinterpret_cast<float4 *>(po + 4 * c1) = pack4<bwd>(val[1]);
+                po += PS;
+                put_word(pxo + wj0, px[0][3], tag, out_j);
+                put_word(pxo + wj1, px[1][3], tag, out_j);
+                if (!bwd) {
+                    put_words2(pxo + wk, px[1][0], px[1][1], tag, out_k);
+                    put_words2(pxo + wk + 2, px[1][2], px[1][3], tag, out_k);
+                } else {
+                    put_words2(pxo + wk, px[1][3], px[1][2], tag, out_k);
+                    put_words2(pxo + wk + 2, px[1][1], px[1][0], tag, out_k);
+                }
+                pxo += XS;
+            };
+            if (np == WT_G) {
+#pragma unroll
+                for (int u = 0; u < WT_G; u++) step(u);
+            } else {
+                for (int u = 0; u < np; u++) step(u);
+            }
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(&mempty[slot]);
+                st_volatile_s32(&rx.cons, g * WT_G + np - 1);   // the steps up to it have been read
+            }
+        }
+        if (to && lane == 0) st_volatile_s32(&rx.cons, S);
+    }
+
+    // block partial of dot(z, r) (the compute warp's lanes in order) and the last-CTA epilogue
+    double part = 0.0;
+    if (MODE == SW_BWD && warp == 0) {
+        part = dot32.value();
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(FULL, part, o);
+    }
+    __shared__ bool last;
+    const unsigned nblocks = (unsigned)(K.nbj * K.nbk);
+    if (tid == 0) {
+        if (MODE == SW_BWD) A.partials[bj + K.nbj * bk] = part;
+        __threadfence();
+        unsigned tk = atomicAdd(A.done_ticket, 1u);
+        last = tk == nblocks - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (MODE == SW_BWD) {
+        double acc = 0.0;
+        for (unsigned q = tid; q < nblocks; q += blockDim.x) acc += __ldcg(A.partials + q);
+        acc = block_reduce<0>(acc);
+        if (tid == 0) {
+            PsCtrl *C = A.ctrl;
+            if (A.init) {
+                C->sigma = acc;
+                C->beta = 0.0;
+            } else {
+                // _solvePressureSystem (pressuresolver.cpp:481-486)
+                C->beta = acc / C->sigma;
+                C->sigma = acc;
+                C->iter += 1;
+                if (C->iter >= C->max_iters) C->done = 1;
+            }
+        }
+    }
+    if (tid == 0) {
+        *A.ticket = 0;
+        *A.done_ticket = 0;
+        A.ctrl->epoch = tag + 1 == 0 ? 1u : tag + 1;
+    }
+}
+
 // -------------------------------------------------------- vector kernels
 
 template <class T>
@@ -1793,6 +2208,26 @@ static bool tri_cl_usable(int S, int ncl) {
     return active1 - 1 >= ncl;
 }
 
+// k_tri_warp's dynamic shared memory limit, raised once per device
+template <int MODE>
+static void launch_tri_warp(Ctx *ctx, const SweepArgs<float> &A) {
+    constexpr int MAXDEV = 64;
+    static bool raised[MAXDEV] = {};
+    static std::mutex mu;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        const bool known = dev >= 0 && dev < MAXDEV;
+        if (!known || !raised[dev]) {
+            cudaFuncSetAttribute(k_tri_warp<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tri_warp_smem<MODE>());
+            if (known) raised[dev] = true;
+        }
+    }
+    k_tri_warp<MODE><<<A.K.nbj * A.K.nbk, WT_THREADS, tri_warp_smem<MODE>(), ctx->stream>>>(A);
+}
+
 template <class T, int MODE, int P, int PE, int CJ, int CK>
 static bool launch_tri_cl(Ctx *ctx, const SweepArgs<T> &A) {
     const int ncl = ((A.K.nbj + CJ - 1) / CJ) * ((A.K.nbk + CK - 1) / CK);
@@ -1856,13 +2291,22 @@ static int launch_sweep(Ctx *ctx, PressureWs &ws, const T *in, T *out, const T *
     } else {
         const int want = ctx->sweep_kernel;
         int ran = 0;
-        // AUTO: the block kernel, the fastest of the three with the receiver warp and gate
-        // (at 256^3 0.24 ms per FP32 backward solve against 0.28 for either cluster shape)
-        if (want == GFS_SWEEP_CLUSTER_4X2 && launch_tri_cl<T, MODE, P, PE, 4, 2>(ctx, A))
+        // AUTO: FP32 solves run the one-warp kernel, FP64 solves the block kernel (the
+        // one-warp kernel is FP32 only; an explicit WARP on an FP64 solve runs BLOCK)
+        bool warp_ran = false;
+        if constexpr (sizeof(T) == 4) {
+            if (want == GFS_SWEEP_AUTO || want == GFS_SWEEP_WARP) {
+                launch_tri_warp<MODE>(ctx, A);
+                ran = GFS_SWEEP_WARP;
+                warp_ran = true;
+            }
+        }
+        if (warp_ran) {
+        } else if (want == GFS_SWEEP_CLUSTER_4X2 && launch_tri_cl<T, MODE, P, PE, 4, 2>(ctx, A))
             ran = GFS_SWEEP_CLUSTER_4X2;
         else if (want == GFS_SWEEP_CLUSTER_2X2 && launch_tri_cl<T, MODE, P, PE, 2, 2>(ctx, A))
             ran = GFS_SWEEP_CLUSTER_2X2;
-        else if (want == GFS_SWEEP_AUTO || want == GFS_SWEEP_BLOCK) {
+        else if (want == GFS_SWEEP_AUTO || want == GFS_SWEEP_BLOCK || want == GFS_SWEEP_WARP) {
             k_tri<T, MODE, P, PE><<<A.K.nbj * A.K.nbk, SPLANE + RX_THREADS, 0, ctx->stream>>>(A);
             ran = GFS_SWEEP_BLOCK;
         } else {

@@ -450,12 +450,16 @@ int gfs_ctx_launch_count(gfs_ctx *ctx, int64_t *count);
 
 /* The MIC(0) triangular solves (PressureSolver::_applyPreconditioner,
    pressuresolver.cpp:304-386) run as i+j+k hyperplane wavefronts over blocks
-   of 16 x 16 pencils.  Three kernels compute the same values in the same order:
-   BLOCK hands block-edge values over through L2 words (four receiver warps per
-   block poll them into shared memory); CLUSTER_4X2 / _2X2 group 4 x 2 or 2 x 2
-   blocks into a thread-block cluster whose blocks hand over through distributed
-   shared memory.  AUTO (the default) runs BLOCK, the fastest of the three on
-   GB300 at 128^3 and 256^3.
+   of 16 x 16 pencils.  BLOCK, CLUSTER_4X2 and CLUSTER_2X2 compute the same values
+   in the same order: BLOCK hands block-edge values over through L2 words (four
+   receiver warps per block poll them into shared memory); CLUSTER_4X2 / _2X2
+   group 4 x 2 or 2 x 2 blocks into a thread-block cluster whose blocks hand over
+   through distributed shared memory.  WARP (FP32 solves only) runs each block
+   with one compute warp and no per-plane barrier, the same per-cell arithmetic
+   and its own (deterministic) summation order of the backward solve's dot
+   product; an FP64 solve asked to run WARP runs BLOCK.  AUTO (the default) runs
+   WARP for FP32 solves and BLOCK for FP64 solves, the fastest on GB300 at 128^3
+   and 256^3.
    A cluster shape set explicitly that cannot run on a grid makes the solve fail
    with GFS_ERR_INVALID.  The preconditioner build always runs its own kernel.
    No counterpart in the reference (its solves are sequential loops). */
@@ -463,9 +467,10 @@ int gfs_ctx_launch_count(gfs_ctx *ctx, int64_t *count);
 #define GFS_SWEEP_BLOCK 1
 #define GFS_SWEEP_CLUSTER_4X2 2
 #define GFS_SWEEP_CLUSTER_2X2 3
+#define GFS_SWEEP_WARP 4
 int gfs_ctx_set_sweep_kernel(gfs_ctx *ctx, int kind);
 /* The kernel the context's last triangular solve ran (GFS_SWEEP_BLOCK /
-   _CLUSTER_4X2 / _CLUSTER_2X2; GFS_SWEEP_AUTO before the first solve). */
+   _CLUSTER_4X2 / _CLUSTER_2X2 / _WARP; GFS_SWEEP_AUTO before the first solve). */
 int gfs_ctx_last_sweep_kernel(gfs_ctx *ctx, int *kind);
 
 /* Bound of every wait of the wavefront kernels, in polls of the awaited word

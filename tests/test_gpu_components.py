@@ -19,17 +19,19 @@ import pytest
 
 from gridfluidsim3d_gb300 import (CLScalarField, MACVelocityField, ParticleAdvector, PressureSolver,
                                   PressureSolverParameters, PRECISION_MIXED, PRECISION_PLAIN, SWEEP_AUTO,
-                                  SWEEP_BLOCK, SWEEP_CLUSTER_2X2, SWEEP_CLUSTER_4X2, scenes)
+                                  SWEEP_BLOCK, SWEEP_CLUSTER_2X2, SWEEP_CLUSTER_4X2, SWEEP_WARP, scenes)
 
 pytestmark = pytest.mark.gpu
 
-SWEEP_KERNELS = {"block": SWEEP_BLOCK, "cluster4x2": SWEEP_CLUSTER_4X2, "cluster2x2": SWEEP_CLUSTER_2X2}
+SWEEP_KERNELS = {"block": SWEEP_BLOCK, "cluster4x2": SWEEP_CLUSTER_4X2, "cluster2x2": SWEEP_CLUSTER_2X2,
+                 "warp": SWEEP_WARP}
 
 
 @pytest.fixture(params=list(SWEEP_KERNELS))
 def sweep_ctx(request, gpu_ctx):
     """The context with each wavefront kernel of the MIC(0) triangular solves in turn
-    (block kernel, 4 x 2 and 2 x 2 clusters); every pressure test runs on all three."""
+    (block kernel, 4 x 2 and 2 x 2 clusters, one-warp kernel: FP32 solves only, FP64
+    solves asked for it run the block kernel); every pressure test runs on each."""
     gpu_ctx.set_sweep_kernel(SWEEP_KERNELS[request.param])
     yield gpu_ctx
     gpu_ctx.set_sweep_kernel(SWEEP_AUTO)

@@ -1,4 +1,4 @@
-"""The three wavefront kernels of the MIC(0) triangular solves, and their bounded waits.
+"""The wavefront kernels of the MIC(0) triangular solves, and their bounded waits.
 
 The triangular solves of PressureSolver::_applyPreconditioner
 (pressuresolver.cpp:304-386) run as i+j+k hyperplane wavefronts over blocks of
@@ -10,8 +10,16 @@ pressures, in FP64 (PLAIN) and in FP32 (MIXED); each is also checked against
 the oracle with the pressure bars (PLAIN: iterations +-1 and 1e-9 relative;
 MIXED: FP64 residual below 1e-6 and 1e-5 relative to an FP64 solve to 1e-12).
 
+The one-warp kernel (FP32 only) computes every cell with the same arithmetic
+but sums the backward solve's dot product in its own order, so it is held to
+the block kernel within FP32 rounding of that dot product (solves capped at 1
+and 3 iterations, where a wrong preconditioner value would show at full size),
+to the oracle bars, to the block kernel's iteration count +-1, and to
+run-to-run bit identity; an FP64 solve asked to run it runs the block kernel.
+
 The grid has 3 x 3 pencil blocks, so every kernel hands over across blocks, and
-the clustered kernels both inside a cluster and between clusters.
+the clustered kernels both inside a cluster and between clusters; its 26 planes
+in i give 56 wavefront steps, so the one-warp kernel's last bulk copy is partial.
 
 The bounded waits: a test hook makes the next wavefront launches wait for an
 exchange tag that no producer writes.  With a small wait limit every waiting
@@ -23,7 +31,7 @@ import pytest
 
 from gridfluidsim3d_gb300 import (GFSError, MACVelocityField, PressureSolver, PressureSolverParameters,
                                   PRECISION_MIXED, PRECISION_PLAIN, SWEEP_AUTO, SWEEP_BLOCK, SWEEP_CLUSTER_2X2,
-                                  SWEEP_CLUSTER_4X2, scenes)
+                                  SWEEP_CLUSTER_4X2, SWEEP_WARP, scenes)
 from gridfluidsim3d_gb300._lib import GFS_ERR_TIMEOUT
 
 pytestmark = pytest.mark.gpu
@@ -50,8 +58,8 @@ def system(oracle_lib):
     return sc, mat, (u, v, w), plain, exact
 
 
-def _solve(ctx, sc, mat, uvw, precision):
-    solver = PressureSolver(ctx, precision=precision)
+def _solve(ctx, sc, mat, uvw, precision, max_iterations=200):
+    solver = PressureSolver(ctx, precision=precision, max_iterations=max_iterations)
     p = solver.solve(PressureSolverParameters(sc.dx, 20.0, sc.dt, mat, MACVelocityField(*sc.dims, sc.dx, *uvw)))
     return p, solver
 
@@ -87,25 +95,59 @@ def test_kernels_match_oracle_and_each_other(kernel_ctx, oracle_lib, system, pre
         assert np.array_equal(p, base_p), f"{name} differs from the block kernel"
 
 
-def test_auto_runs_the_block_kernel(kernel_ctx, system):
+def test_auto_runs_warp_for_fp32_and_block_for_fp64(kernel_ctx, system):
     sc, mat, uvw, _, _ = system
     kernel_ctx.set_sweep_kernel(SWEEP_AUTO)
-    for precision in (PRECISION_MIXED, PRECISION_PLAIN):
+    for precision, want in ((PRECISION_MIXED, SWEEP_WARP), (PRECISION_PLAIN, SWEEP_BLOCK)):
         _solve(kernel_ctx, sc, mat, uvw, precision)
-        assert kernel_ctx.last_sweep_kernel() == SWEEP_BLOCK
+        assert kernel_ctx.last_sweep_kernel() == want
+
+
+def test_warp_kernel_against_block_kernel_and_oracle(kernel_ctx, oracle_lib, system):
+    O = oracle_lib
+    sc, mat, uvw, (want, it_ref, _), (exact, _, _) = system
+    # capped solves: the preconditioner values are the block kernel's, the dot product differs in rounding
+    for iters in (1, 3):
+        kernel_ctx.set_sweep_kernel(SWEEP_BLOCK)
+        pb, _ = _solve(kernel_ctx, sc, mat, uvw, PRECISION_MIXED, max_iterations=iters)
+        kernel_ctx.set_sweep_kernel(SWEEP_WARP)
+        pw, _ = _solve(kernel_ctx, sc, mat, uvw, PRECISION_MIXED, max_iterations=iters)
+        assert kernel_ctx.last_sweep_kernel() == SWEEP_WARP
+        assert np.abs(pb).max() > 0
+        rel = np.abs(pw - pb).max() / np.abs(pb).max()
+        assert rel < 1e-5, (iters, rel)
+    # full solves
+    kernel_ctx.set_sweep_kernel(SWEEP_BLOCK)
+    pb, sb = _solve(kernel_ctx, sc, mat, uvw, PRECISION_MIXED)
+    kernel_ctx.set_sweep_kernel(SWEEP_WARP)
+    pw, sw = _solve(kernel_ctx, sc, mat, uvw, PRECISION_MIXED)
+    pw2, sw2 = _solve(kernel_ctx, sc, mat, uvw, PRECISION_MIXED)
+    assert np.array_equal(pw, pw2) and sw.iterations == sw2.iterations      # deterministic
+    assert abs(sw.iterations - sb.iterations) <= 1, (sw.iterations, sb.iterations)
+    assert O.pressure_residual(sc.dims, sc.dx, 20.0, sc.dt, mat, *uvw, pw) < 1e-6
+    assert np.abs(pw - exact).max() / np.abs(exact).max() < 1e-5
+    # FP64: the block kernel runs, bit for bit
+    kernel_ctx.set_sweep_kernel(SWEEP_BLOCK)
+    qb, tb = _solve(kernel_ctx, sc, mat, uvw, PRECISION_PLAIN)
+    kernel_ctx.set_sweep_kernel(SWEEP_WARP)
+    qw, tw = _solve(kernel_ctx, sc, mat, uvw, PRECISION_PLAIN)
+    assert kernel_ctx.last_sweep_kernel() == SWEEP_BLOCK
+    assert np.array_equal(qw, qb) and tw.iterations == tb.iterations
 
 
 def test_invalid_kernel_is_rejected(kernel_ctx):
     with pytest.raises(GFSError):
         kernel_ctx.set_sweep_kernel(7)
+    with pytest.raises(GFSError):
+        kernel_ctx.set_sweep_kernel(5)
 
 
 @pytest.mark.parametrize("precision", [PRECISION_PLAIN, PRECISION_MIXED], ids=["plain_fp64", "mixed_fp32"])
-@pytest.mark.parametrize("kernel", list(KERNELS))
+@pytest.mark.parametrize("kernel", list(KERNELS) + ["warp"])
 def test_wait_timeout_is_reported_and_the_context_recovers(kernel_ctx, oracle_lib, system, kernel, precision):
     O = oracle_lib
     sc, mat, uvw, (want, it_ref, _), (exact, _, _) = system
-    kernel_ctx.set_sweep_kernel(KERNELS[kernel])
+    kernel_ctx.set_sweep_kernel(dict(KERNELS, warp=SWEEP_WARP)[kernel])
     kernel_ctx.set_wait_limit(2000)
     # the build, forward and backward sweeps of the first iteration look for a tag nobody writes
     kernel_ctx.inject_wait_timeout(3)
