@@ -1352,8 +1352,9 @@ static size_t tri_cl_smem(int S) {
 // edge word of its class is in the ring.  Slots of cells outside the grid hold 0
 // in the input and preconditioner vectors, so such a cell computes +-0 without a
 // select and hands over +-0.  Arithmetic per cell is k_tri's; the backward
-// solve's dot(z, r) sums each lane's eight products per step before its
-// compensated running sum (deterministic; its rounding differs from k_tri's).
+// solve's dot(z, r) sums each lane's eight rounded products of a step pairwise
+// before its compensated running sum (deterministic; its rounding differs from
+// k_tri's per-pencil sums; measured at 256^3 it takes as many inner iterations).
 static constexpr int WT_G = 8;                             // planes per bulk copy
 static constexpr int WT_NG = 4;                            // copies in flight
 static constexpr int WT_THREADS = 32 + RX_THREADS + 32;    // compute warp, receiver warps, loader warp
@@ -1655,7 +1656,6 @@ __global__ void __launch_bounds__(WT_THREADS, 1) k_tri_warp(SweepArgs<float> A) 
                     nk[1][p] = __shfl_sync(FULL, send, (lane - 4) & 31);
                 }
                 float val[2][4];
-                float part = 0.f;
 #pragma unroll
                 for (int r = 0; r < 2; r++)
 #pragma unroll
@@ -1671,10 +1671,17 @@ __global__ void __launch_bounds__(WT_THREADS, 1) k_tri_warp(SweepArgs<float> A) 
                                                         Op::mul(m, nk[r][p])),
                                                 pc[r][p]);
                             px[r][p] = val[r][p];
-                            part = fmaf(val[r][p], rv[r][p], part);
                         }
                     }
-                if (bwd) dot32.add(part);
+                if (bwd) {
+                    // dot(z, r): the eight rounded products summed pairwise, then the compensated running sum
+                    float pr[8];
+#pragma unroll
+                    for (int r = 0; r < 2; r++)
+#pragma unroll
+                        for (int p = 0; p < 4; p++) pr[4 * r + p] = val[r][p] * rv[r][p];
+                    dot32.add(((pr[0] + pr[1]) + (pr[2] + pr[3])) + ((pr[4] + pr[5]) + (pr[6] + pr[7])));
+                }
                 *reinterpret_cast<float4 *>(po + 4 * c0) = pack4<bwd>(val[0]);
                 *reinterpret_cast<float4 *>(po + 4 * c1) = pack4<bwd>(val[1]);
                 po += PS;
