@@ -13,8 +13,9 @@ PIC/FLIP update, RK4 advection with collisions, particle re-sort.
 value      substeps/s of the MIXED-precision form, state resident in HBM
            (inputs of 40M particles x 32 B >> L2, so no flush is needed).
 plain      the same K substeps with the FP64 (PLAIN) form, from the same state.
-e2e        substeps/s through gfs_sim_step_host: particles copied from pinned
-           host memory to the device and back inside every step.
+e2e        substeps/s through gfs_sim_step_host: particles from pinned host
+           memory into the device and back inside every step (the pack / unpack
+           kernels read and write the pinned buffers in place over the host link).
 roofline   the dominant kernel class: algorithmic bytes per launch / average
            device time per working launch, from CUDA events on the library's
            stream around every launch of a second timed pass of the same K steps
@@ -83,7 +84,7 @@ BYTES = {
 }
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# FP32 sweeps (k_tri) on this exact workload, from one single-pass ncu capture of
+# FP32 sweeps (k_tri_warp) on this exact workload, from one single-pass ncu capture of
 # two forward / backward pairs of this bench's mixed run.  A sweep streams every
 # plane of each block that holds fluid (134 of the 256 blocks here), air and
 # padding slots included.

@@ -152,24 +152,77 @@ static int download_padded(Ctx *ctx, const T *d_padded, const GridDim &g, T *h, 
 
 // ------------------------------------------------------ particle packing
 
-__global__ void k_pack_particles(const float *__restrict__ p3, const float *__restrict__ v3,
-                                 const uint32_t *__restrict__ ids, long long n, float4 *__restrict__ pos,
-                                 float4 *__restrict__ vel) {
-    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (q >= n) return;
-    uint32_t id = ids ? ids[q] : (uint32_t)q;
-    pos[q] = make_float4(p3[3 * q], p3[3 * q + 1], p3[3 * q + 2], __uint_as_float(id));
-    vel[q] = v3 ? make_float4(v3[3 * q], v3[3 * q + 1], v3[3 * q + 2], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+// xyz triples <-> the device's float4 particles (id in pos.w).  A block of 256
+// threads moves 1024 particles; with 16-byte aligned triples (vec) and a full
+// block, the block's triples travel through shared memory so that every warp
+// load or store instruction covers 512 contiguous bytes -- whole lines, which is
+// what the host link needs when the triples are host memory read or written in
+// place (scattered 16-byte pieces ran at a third of the link rate) -- else one
+// particle per thread, one float at a time.
+static constexpr int PK_THREADS = 256, PK_PER = 4 * PK_THREADS;   // particles per block
+
+__device__ __forceinline__ void copy_block16(float4 *__restrict__ dst, const float4 *__restrict__ src, int n16) {
+    for (int i = threadIdx.x; i < n16; i += PK_THREADS) dst[i] = src[i];
 }
 
-__global__ void k_unpack_particles(const float4 *__restrict__ pos, const float4 *__restrict__ vel, long long n,
-                                   float *__restrict__ p3, float *__restrict__ v3, uint32_t *__restrict__ ids) {
-    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (q >= n) return;
-    float4 p = pos[q], v = vel[q];
-    p3[3 * q] = p.x; p3[3 * q + 1] = p.y; p3[3 * q + 2] = p.z;
-    v3[3 * q] = v.x; v3[3 * q + 1] = v.y; v3[3 * q + 2] = v.z;
-    ids[q] = __float_as_uint(p.w);
+__global__ void __launch_bounds__(PK_THREADS) k_pack_particles(const float *__restrict__ p3,
+                                                               const float *__restrict__ v3,
+                                                               const uint32_t *__restrict__ ids, long long n,
+                                                               float4 *__restrict__ pos, float4 *__restrict__ vel,
+                                                               int vec) {
+    __shared__ __align__(16) float sp[3 * PK_PER], sv[3 * PK_PER];
+    const long long b0 = (long long)blockIdx.x * PK_PER;
+    const int t = threadIdx.x;
+    if (vec && b0 + PK_PER <= n) {
+        copy_block16(reinterpret_cast<float4 *>(sp), reinterpret_cast<const float4 *>(p3 + 3 * b0), 3 * PK_PER / 4);
+        if (v3) copy_block16(reinterpret_cast<float4 *>(sv), reinterpret_cast<const float4 *>(v3 + 3 * b0), 3 * PK_PER / 4);
+        __syncthreads();
+        for (int k = t; k < PK_PER; k += PK_THREADS) {   // consecutive threads, consecutive particles
+            const long long q = b0 + k;
+            const uint32_t id = ids ? ids[q] : (uint32_t)q;
+            pos[q] = make_float4(sp[3 * k], sp[3 * k + 1], sp[3 * k + 2], __uint_as_float(id));
+            vel[q] = v3 ? make_float4(sv[3 * k], sv[3 * k + 1], sv[3 * k + 2], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        return;
+    }
+    for (long long q = b0 + t; q < b0 + PK_PER && q < n; q += PK_THREADS) {
+        const uint32_t id = ids ? ids[q] : (uint32_t)q;
+        pos[q] = make_float4(p3[3 * q], p3[3 * q + 1], p3[3 * q + 2], __uint_as_float(id));
+        vel[q] = v3 ? make_float4(v3[3 * q], v3[3 * q + 1], v3[3 * q + 2], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+__global__ void __launch_bounds__(PK_THREADS) k_unpack_particles(const float4 *__restrict__ pos,
+                                                                 const float4 *__restrict__ vel, long long n,
+                                                                 float *__restrict__ p3, float *__restrict__ v3,
+                                                                 uint32_t *__restrict__ ids, int vec) {
+    __shared__ __align__(16) float sp[3 * PK_PER], sv[3 * PK_PER];
+    const long long b0 = (long long)blockIdx.x * PK_PER;
+    const int t = threadIdx.x;
+    if (vec && b0 + PK_PER <= n) {
+        for (int k = t; k < PK_PER; k += PK_THREADS) {
+            const long long q = b0 + k;
+            const float4 p = pos[q], v = vel[q];
+            sp[3 * k] = p.x; sp[3 * k + 1] = p.y; sp[3 * k + 2] = p.z;
+            sv[3 * k] = v.x; sv[3 * k + 1] = v.y; sv[3 * k + 2] = v.z;
+            ids[q] = __float_as_uint(p.w);
+        }
+        __syncthreads();
+        copy_block16(reinterpret_cast<float4 *>(p3 + 3 * b0), reinterpret_cast<const float4 *>(sp), 3 * PK_PER / 4);
+        copy_block16(reinterpret_cast<float4 *>(v3 + 3 * b0), reinterpret_cast<const float4 *>(sv), 3 * PK_PER / 4);
+        return;
+    }
+    for (long long q = b0 + t; q < b0 + PK_PER && q < n; q += PK_THREADS) {
+        const float4 p = pos[q], v = vel[q];
+        p3[3 * q] = p.x; p3[3 * q + 1] = p.y; p3[3 * q + 2] = p.z;
+        v3[3 * q] = v.x; v3[3 * q + 1] = v.y; v3[3 * q + 2] = v.z;
+        ids[q] = __float_as_uint(p.w);
+    }
+}
+
+static bool all_a16(const void *a, const void *b, const void *c) {
+    auto ok = [](const void *q) { return q == nullptr || ((uintptr_t)q & 15u) == 0; };
+    return ok(a) && ok(b) && ok(c);
 }
 
 static bool valid_dims(int ni, int nj, int nk) {
@@ -235,6 +288,32 @@ static int sim_init(Sim *s, Ctx *ctx, int ni, int nj, int nk, double dx, int64_t
     return GFS_OK;
 }
 
+// The device address of a host buffer that the device can read and write in
+// place -- page-locked and mapped (cudaHostAlloc / cudaHostRegister) for the
+// current device, the whole range in one registration -- else nullptr (pageable
+// or managed memory goes through a staged copy).  On GB300 the device then
+// reaches it over the NVLink-C2C host link from inside the pack / unpack kernels.
+static void *mapped_host(const void *h, size_t bytes) {
+    if (!h || bytes == 0) return nullptr;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    cudaPointerAttributes a0, a1;
+    if (cudaPointerGetAttributes(&a0, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a0.type != cudaMemoryTypeHost || a0.devicePointer == nullptr || a0.device != dev) return nullptr;
+    const char *last = (const char *)h + bytes - 1;
+    if (cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a1.type != cudaMemoryTypeHost || a1.devicePointer == nullptr ||
+        (const char *)a1.devicePointer - (const char *)a0.devicePointer != (ptrdiff_t)(bytes - 1))
+        return nullptr;
+    return a0.devicePointer;
+}
+
 static int sim_set_particles(Sim *s, const float *hp, const float *hv, const uint32_t *hid, int64_t n) {
     Ctx *ctx = s->ctx;
     if (n < 0 || n > s->capacity) {
@@ -247,15 +326,22 @@ static int sim_set_particles(Sim *s, const float *hp, const float *hv, const uin
         return GFS_ERR_INVALID;
     }
     cudaStream_t st = ctx->stream;
-    // stage xyz triples in the alternate buffers (16 B per particle >= 12 B)
-    float *p3 = s->pos_alt.as<float>(), *v3 = s->vel_alt.as<float>();
-    uint32_t *ids = s->key.as<uint32_t>();
+    // xyz triples: read in place from mapped host buffers, else staged in the
+    // alternate buffers (16 B per particle >= 12 B)
+    const float *p3 = s->pos_alt.as<float>(), *v3 = s->vel_alt.as<float>();
+    const uint32_t *ids = s->key.as<uint32_t>();
     if (n > 0) {
-        GFS_CUDA_CHECK(cudaMemcpyAsync(p3, hp, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, st));
-        if (hv) GFS_CUDA_CHECK(cudaMemcpyAsync(v3, hv, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, st));
-        if (hid) GFS_CUDA_CHECK(cudaMemcpyAsync(ids, hid, (size_t)n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-        k_pack_particles<<<grid_blocks(n, 256), 256, 0, st>>>(p3, hv ? v3 : nullptr, hid ? ids : nullptr, n,
-                                                              s->pos.as<float4>(), s->vel.as<float4>());
+        const size_t b3 = (size_t)n * 3 * sizeof(float), b1 = (size_t)n * sizeof(uint32_t);
+        if (const void *d = mapped_host(hp, b3)) p3 = (const float *)d;
+        else GFS_CUDA_CHECK(cudaMemcpyAsync(s->pos_alt.p, hp, b3, cudaMemcpyHostToDevice, st));
+        if (!hv) v3 = nullptr;
+        else if (const void *d = mapped_host(hv, b3)) v3 = (const float *)d;
+        else GFS_CUDA_CHECK(cudaMemcpyAsync(s->vel_alt.p, hv, b3, cudaMemcpyHostToDevice, st));
+        if (!hid) ids = nullptr;
+        else if (const void *d = mapped_host(hid, b1)) ids = (const uint32_t *)d;
+        else GFS_CUDA_CHECK(cudaMemcpyAsync(s->key.p, hid, b1, cudaMemcpyHostToDevice, st));
+        k_pack_particles<<<grid_blocks(n, PK_PER), PK_THREADS, 0, st>>>(p3, v3, ids, n, s->pos.as<float4>(),
+                                                                        s->vel.as<float4>(), all_a16(p3, v3, ids));
         ctx->launches++;
         GFS_LAUNCH_CHECK();
     }
@@ -282,9 +368,9 @@ int sim_stage_xyz(Sim *s, int64_t *n_out) {
     GFS_CUDA_CHECK(cudaStreamSynchronize(st));
     *n_out = hn;
     if (hn > 0) {
-        k_unpack_particles<<<grid_blocks(hn, 256), 256, 0, st>>>(s->pos.as<float4>(), s->vel.as<float4>(), hn,
-                                                                 s->pos_alt.as<float>(), s->vel_alt.as<float>(),
-                                                                 s->key.as<uint32_t>());
+        k_unpack_particles<<<grid_blocks(hn, PK_PER), PK_THREADS, 0, st>>>(
+            s->pos.as<float4>(), s->vel.as<float4>(), hn, s->pos_alt.as<float>(), s->vel_alt.as<float>(),
+            s->key.as<uint32_t>(), 1);
         ctx->launches++;
         GFS_LAUNCH_CHECK();
     }
@@ -302,8 +388,9 @@ int sim_unstage_xyz(Sim *s, int64_t n) {
         return GFS_ERR_INVALID;
     }
     if (n > 0) {
-        k_pack_particles<<<grid_blocks(n, 256), 256, 0, st>>>(s->pos_alt.as<float>(), s->vel_alt.as<float>(),
-                                                              nullptr, n, s->pos.as<float4>(), s->vel.as<float4>());
+        k_pack_particles<<<grid_blocks(n, PK_PER), PK_THREADS, 0, st>>>(s->pos_alt.as<float>(),
+                                                                        s->vel_alt.as<float>(), nullptr, n,
+                                                                        s->pos.as<float4>(), s->vel.as<float4>(), 1);
         ctx->launches++;
         GFS_LAUNCH_CHECK();
     }
@@ -329,15 +416,21 @@ static int sim_get_particles(Sim *s, float *hp, float *hv, uint32_t *hid, int64_
     long long n = hn;
     if (n_out) *n_out = n;
     if (n > 0 && (hp || hv || hid)) {
+        // written in place into mapped host buffers, else staged and copied
+        const size_t b3 = (size_t)n * 3 * sizeof(float), b1 = (size_t)n * sizeof(uint32_t);
         float *p3 = s->pos_alt.as<float>(), *v3 = s->vel_alt.as<float>();
         uint32_t *ids = s->key.as<uint32_t>();
-        k_unpack_particles<<<grid_blocks(n, 256), 256, 0, st>>>(s->pos.as<float4>(), s->vel.as<float4>(), n, p3,
-                                                                v3, ids);
+        float *mp = (float *)mapped_host(hp, b3), *mv = (float *)mapped_host(hv, b3);
+        uint32_t *mi = (uint32_t *)mapped_host(hid, b1);
+        float *op = mp ? mp : p3, *ov = mv ? mv : v3;
+        uint32_t *oi = mi ? mi : ids;
+        k_unpack_particles<<<grid_blocks(n, PK_PER), PK_THREADS, 0, st>>>(
+            s->pos.as<float4>(), s->vel.as<float4>(), n, op, ov, oi, all_a16(op, ov, oi));
         ctx->launches++;
         GFS_LAUNCH_CHECK();
-        if (hp) GFS_CUDA_CHECK(cudaMemcpyAsync(hp, p3, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
-        if (hv) GFS_CUDA_CHECK(cudaMemcpyAsync(hv, v3, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
-        if (hid) GFS_CUDA_CHECK(cudaMemcpyAsync(hid, ids, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        if (hp && !mp) GFS_CUDA_CHECK(cudaMemcpyAsync(hp, p3, b3, cudaMemcpyDeviceToHost, st));
+        if (hv && !mv) GFS_CUDA_CHECK(cudaMemcpyAsync(hv, v3, b3, cudaMemcpyDeviceToHost, st));
+        if (hid && !mi) GFS_CUDA_CHECK(cudaMemcpyAsync(hid, ids, b1, cudaMemcpyDeviceToHost, st));
         GFS_CUDA_CHECK(cudaStreamSynchronize(st));
     }
     return GFS_OK;

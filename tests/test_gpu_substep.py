@@ -111,6 +111,46 @@ def test_host_step_matches_device_step(gpu_ctx):
     assert np.array_equal(ids[:n], dids) and np.array_equal(pos[:n], dpos) and np.array_equal(vel[:n], dvel)
 
 
+@pytest.mark.parametrize("layout", ["all_pinned", "mixed"])
+def test_host_step_with_pinned_buffers(gpu_ctx, layout):
+    """update_host with page-locked (mapped) host buffers: the pack / unpack kernels
+    read and write them in place instead of a staged copy; two steps, each handing
+    the previous one's output back, give the device path's particles bit for bit,
+    with every buffer pinned and with pinned positions beside pageable velocities
+    and ids."""
+    torch = pytest.importorskip("torch")
+    sc = scenes.random_box(dims=(16, 12, 14), seed=3)
+    sim = FluidSimulation(*sc.dims, sc.dx, max_particles=sc.num_particles, ctx=gpu_ctx)
+    sim.set_material_grid(sc.mat)
+    sim.set_marker_particles(sc.pos, sc.vel, sc.ids)
+    for _ in range(2):
+        sim.update(sc.dt)
+    dpos, dvel, dids = sim.get_marker_particles()
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float32 if a.dtype == np.float32 else torch.int32, pin_memory=True)
+        v = t.numpy().view(a.dtype)
+        v[:] = a
+        return t, v
+
+    keep = []
+    tp, pos = pinned(sc.pos)
+    keep.append(tp)
+    if layout == "all_pinned":
+        tv, vel = pinned(sc.vel)
+        ti, ids = pinned(sc.ids)
+        keep += [tv, ti]
+    else:
+        vel, ids = sc.vel.copy(), sc.ids.copy()
+    sim2 = FluidSimulation(*sc.dims, sc.dx, max_particles=sc.num_particles, ctx=gpu_ctx)
+    sim2.set_material_grid(sc.mat)
+    n = len(pos)
+    for _ in range(2):
+        n, _ = sim2.update_host(sc.dt, pos[:n], vel[:n], ids[:n])
+    assert n == len(dids)
+    assert np.array_equal(ids[:n], dids) and np.array_equal(pos[:n], dpos) and np.array_equal(vel[:n], dvel)
+
+
 def test_invalid_dt_raises(gpu_ctx):
     from gridfluidsim3d_gb300 import GFSError
     sc = scenes.random_box(dims=(10, 10, 10), seed=1)
