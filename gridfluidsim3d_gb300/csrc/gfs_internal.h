@@ -110,6 +110,8 @@ struct PressureWs {
     DevMem xch;                  // block-boundary exchange words of the wavefronts
     DevMem nbstd, nbsk;          // MIC(0) neighbour bits, padded cell and skewed layouts
     DevMem blkf;                 // per skew block: 1 if it holds a fluid cell
+    DevMem slist, soff, stmp;    // strips holding fluid (uint32 indices, in order); per-strip scan, scan temp
+    DevMem snum;                 // uint32: the length of slist
     size_t nblocks_red = 0;      // blocks of the reduction kernels
     long long allocated_for = -1;
     bool mixed_alloc = false;

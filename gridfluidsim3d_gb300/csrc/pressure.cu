@@ -1764,6 +1764,8 @@ struct VecArgs {
     double *partials;
     PsCtrl *ctrl;
     int mixed;
+    const unsigned *slist;   // the strips (of Strip<T>::W slots) that hold fluid, in order
+    const unsigned *snum;    // their number
 };
 
 // x at the six neighbours of slot q in the skewed layout, in the reference's
@@ -1789,9 +1791,12 @@ __device__ __forceinline__ T neighbour_sum(const Skew &K, const T *__restrict__ 
 // consecutive slots of one row (fixed plane s and kl) of a pencil block -- 8
 // FP32 or 4 FP64 slots.  A strip costs one flag load and two 16-byte loads per
 // operand, all issued together, so the kernels stream at HBM rate instead of
-// waiting on a byte load before each slot's operands.  Strips without fluid are
-// skipped; stores stay per slot and on fluid slots only, so the results are those
-// of the slot-wise loops in the reference (pressuresolver.cpp:388-486) bit for bit.
+// waiting on a byte load before each slot's operands.  The kernels walk the list
+// of strips that hold fluid (built once per solve, in strip order; at 256^3 about
+// a third of all strips), so strips without fluid cost neither a flag load nor a
+// thread.  Stores stay per slot and on fluid slots only, so the per-slot results
+// are those of the slot-wise loops in the reference (pressuresolver.cpp:388-486)
+// bit for bit; the reductions sum in the walk's fixed order.
 
 template <class T>
 struct Strip {
@@ -1937,6 +1942,51 @@ __device__ __forceinline__ void neighbour_sum_strip(const Skew &K, const T *__re
     }
 }
 
+// The strips that hold a fluid slot, in strip order, for the per-iteration vector
+// kernels (built once per solve: the fluid set is fixed during it).  off[u] = 1 if
+// strip u holds fluid; an exclusive scan of off turns it into list positions.
+template <class T>
+__global__ void __launch_bounds__(RED_THREADS) k_strip_mark(Skew K, const uint8_t *__restrict__ fsk,
+                                                            unsigned *__restrict__ off) {
+    constexpr int W = Strip<T>::W;
+    const unsigned nstrip = (unsigned)(K.size / W);
+    for (unsigned u = blockIdx.x * blockDim.x + threadIdx.x; u <= nstrip; u += gridDim.x * blockDim.x) {
+        if (u == nstrip) {
+            off[u] = 0u;
+            continue;
+        }
+        StripFlags<T> f;
+        f.load(fsk, (long long)u * W);
+        off[u] = f.any() ? 1u : 0u;
+    }
+}
+__global__ void __launch_bounds__(RED_THREADS) k_strip_list(unsigned nstrip, const unsigned *__restrict__ off,
+                                                            unsigned *__restrict__ list, unsigned *__restrict__ num) {
+    for (unsigned u = blockIdx.x * blockDim.x + threadIdx.x; u < nstrip; u += gridDim.x * blockDim.x)
+        if (off[u + 1] != off[u]) list[off[u]] = u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *num = off[nstrip];
+}
+
+// The next strip of a thread's walk over the list: loaded one step ahead, so the
+// list read does not sit in front of the strip's own loads.
+struct StripWalk {
+    const unsigned *list;
+    unsigned n, i, stride, next;
+    __device__ __forceinline__ StripWalk(const unsigned *l, const unsigned *num) : list(l) {
+        n = *num;
+        i = blockIdx.x * blockDim.x + threadIdx.x;
+        stride = gridDim.x * blockDim.x;
+        next = i < n ? list[i] : 0u;
+    }
+    __device__ __forceinline__ bool more() const { return i < n; }
+    __device__ __forceinline__ unsigned take() {
+        const unsigned u = next;
+        i += stride;
+        if (i < n) next = list[i];
+        return u;
+    }
+};
+
 // As = A s and dot(As, s) -> alpha (pressuresolver.cpp:388-426, :472-473)
 template <class T>
 __global__ void __launch_bounds__(RED_THREADS) k_matvec(VecArgs<T> A, const T *__restrict__ s,
@@ -1947,12 +1997,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_matvec(VecArgs<T> A, const T *_
     const Skew &K = A.K;
     double dot = 0.0;   // FP64 operands
     Acc2f dot32;        // FP32 operands: compensated
-    const unsigned nstrip = (unsigned)(K.size / W);
-    for (unsigned u = blockIdx.x * blockDim.x + threadIdx.x; u < nstrip; u += gridDim.x * blockDim.x) {
-        const StripPos P = strip_pos<T>(K, u);
+    for (StripWalk sw(A.slist, A.snum); sw.more();) {
+        const StripPos P = strip_pos<T>(K, sw.take());
         StripFlags<T> f;
         f.load(A.fsk, P.q0);
-        if (!f.any()) continue;
         T xc[W], val[W];
         load_strip<T>(xc, s + P.q0);
         neighbour_sum_strip<T>(K, s, P, val);
@@ -1985,12 +2033,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_axpy(VecArgs<T> A, T *__restric
     if (C->done) return;
     const T alpha = (T)C->alpha, nalpha = (T)(-C->alpha);
     T mx = T(0);
-    const unsigned nstrip = (unsigned)(A.K.size / W);
-    for (unsigned u = blockIdx.x * blockDim.x + threadIdx.x; u < nstrip; u += gridDim.x * blockDim.x) {
-        const long long q0 = (long long)u * W;
+    for (StripWalk sw(A.slist, A.snum); sw.more();) {
+        const long long q0 = (long long)sw.take() * W;
         StripFlags<T> f;
         f.load(A.fsk, q0);
-        if (!f.any()) continue;
         T pv[W], sv[W], rv[W], av[W];
         load_strip<T>(pv, p + q0);
         load_strip<T>(sv, s + q0);
@@ -2025,12 +2071,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_update_s(VecArgs<T> A, const T 
     constexpr int W = Strip<T>::W;
     if (A.ctrl->done) return;
     const T beta = (T)A.ctrl->beta;
-    const unsigned nstrip = (unsigned)(A.K.size / W);
-    for (unsigned u = blockIdx.x * blockDim.x + threadIdx.x; u < nstrip; u += gridDim.x * blockDim.x) {
-        const long long q0 = (long long)u * W;
+    for (StripWalk sw(A.slist, A.snum); sw.more();) {
+        const long long q0 = (long long)sw.take() * W;
         StripFlags<T> f;
         f.load(A.fsk, q0);
-        if (!f.any()) continue;
         T zv[W], sv[W];
         load_strip<T>(zv, z + q0);
         load_strip<T>(sv, s + q0);
@@ -2158,6 +2202,12 @@ static int ensure_ws(Ctx *ctx, PressureWs &ws, const Grids &g, bool mixed) {
         GFS_CUDA_CHECK(cudaMemsetAsync(ws.xch.p, 0, ws.xch.bytes, ctx->stream));
         if (ws.nbstd.alloc((size_t)n * sizeof(uint16_t)) || ws.nbsk.alloc((size_t)K.size * sizeof(uint16_t)))
             return GFS_ERR_NOMEM;
+        // strip list: at most K.size / 4 strips (FP64 strips of 4 slots)
+        const size_t maxstrip = (size_t)(K.size / 4);
+        if (ws.slist.alloc(maxstrip * sizeof(unsigned)) || ws.soff.alloc((maxstrip + 1) * sizeof(unsigned)) ||
+            ws.stmp.alloc(scan_temp_elems((long long)maxstrip + 1) * sizeof(unsigned)) || ws.snum.alloc(sizeof(unsigned)))
+            return GFS_ERR_NOMEM;
+        GFS_CUDA_CHECK(cudaMemsetAsync(ws.snum.p, 0, sizeof(unsigned), ctx->stream));
         GFS_CUDA_CHECK(cudaMemsetAsync(ws.nbsk.p, 0, ws.nbsk.bytes, ctx->stream));
         ws.allocated_for = n;
         ws.mixed_alloc = false;
@@ -2338,6 +2388,8 @@ static VecArgs<T> vec_args(PressureWs &ws, double scale, int mixed) {
     A.partials = ws.partials.as<double>();
     A.ctrl = ws.ctrl.as<PsCtrl>();
     A.mixed = mixed;
+    A.slist = ws.slist.as<unsigned>();
+    A.snum = ws.snum.as<unsigned>();
     return A;
 }
 
@@ -2388,12 +2440,31 @@ static int read_ctrl(Ctx *ctx, PressureWs &ws, PsCtrl *h) {
 // inner PCG in FP32 with FP64 reliable updates of the residual.  Fills the
 // reference-numbered iteration count, the final max-norm residual, the number
 // of FP64 updates and of forward (= backward) MIC(0) solves.
+// The list of strips (of Strip<T>::W slots) that hold fluid, for this solve's vector kernels.
+template <class T>
+static int build_strip_list(Ctx *ctx, PressureWs &ws, const Skew &K) {
+    const long long nstrip = K.size / Strip<T>::W;
+    cudaStream_t st = ctx->stream;
+    unsigned nb = (unsigned)ws.nblocks_red;
+    unsigned *off = ws.soff.as<unsigned>();
+    k_strip_mark<T><<<nb, RED_THREADS, 0, st>>>(K, ws.fsk.as<uint8_t>(), off);
+    ctx->launches++;
+    GFS_LAUNCH_CHECK();
+    int rc = exclusive_scan_u32(ctx, off, off, nstrip + 1, ws.stmp.as<unsigned>(), st);
+    if (rc) return rc;
+    k_strip_list<<<nb, RED_THREADS, 0, st>>>((unsigned)nstrip, off, ws.slist.as<unsigned>(), ws.snum.as<unsigned>());
+    ctx->launches++;
+    GFS_LAUNCH_CHECK();
+    return GFS_OK;
+}
+
 static int run_cg(Ctx *ctx, PressureWs &ws, const Skew &K, double scale, bool mixed, double tol, int max_iters,
                   PsCtrl &h, int &iterations, double &final_res, int &refinements, int &sweeps) {
     cudaStream_t st = ctx->stream;
     PsCtrl *C = ws.ctrl.as<PsCtrl>();
     unsigned nb = (unsigned)ws.nblocks_red;
-    int rc = GFS_OK;
+    int rc = mixed ? build_strip_list<float>(ctx, ws, K) : build_strip_list<double>(ctx, ws, K);
+    if (rc) return rc;
     // MIC(0) preconditioner (pressuresolver.cpp:246-302): FP64 for PLAIN, FP32 for the MIXED inner solve
     if (mixed) rc = launch_sweep<float, SW_PRECON>(ctx, ws, nullptr, ws.precon32.as<float>(), nullptr, nullptr,
                                                    nullptr, scale, 0);
