@@ -111,18 +111,37 @@ __global__ void k_cap_counts(const uint32_t *__restrict__ offset, long long ncel
     cnt[c] = m < (uint32_t)cap ? m : (uint32_t)cap;
 }
 
+// One thread per particle of the sorted set: the particle's cell (the sort's own
+// formula, k_keys) and its rank in the cell; the first `cap` of each cell (the
+// smallest ids) move to the capped offsets, in order -- coalesced reads and writes.
 __global__ void k_cap_copy(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                            const uint32_t *__restrict__ off_in, const uint32_t *__restrict__ off_out,
-                           long long ncells, float4 *__restrict__ pos_out,
-                           float4 *__restrict__ vel_out, uint32_t *__restrict__ num) {
-    long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (c >= ncells) return;
-    uint32_t b = off_in[c], o = off_out[c], m = off_out[c + 1] - o;
-    for (uint32_t a = 0; a < m; a++) {
-        pos_out[o + a] = pos[b + a];
-        vel_out[o + a] = vel[b + a];
+                           long long ncells, long long n, GridDim c, double invdx_d, float invdx_f, int pow2,
+                           int cap, float4 *__restrict__ pos_out, float4 *__restrict__ vel_out,
+                           uint32_t *__restrict__ num) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p == 0) num[0] = off_out[ncells];
+    if (p >= n) return;
+    const float4 x = pos[p];
+    int i, j, k;
+    if (pow2) {
+        i = (int)floorf(x.x * invdx_f);
+        j = (int)floorf(x.y * invdx_f);
+        k = (int)floorf(x.z * invdx_f);
+    } else {
+        i = (int)floor((double)x.x * invdx_d);
+        j = (int)floor((double)x.y * invdx_d);
+        k = (int)floor((double)x.z * invdx_d);
     }
-    if (c == ncells - 1) num[0] = off_out[ncells];
+    if (!c.in(i, j, k)) return;   // never for a sorted set
+    const uint32_t kk = (uint32_t)i + (uint32_t)c.nx * ((uint32_t)j + (uint32_t)c.ny * (uint32_t)k);
+    const uint32_t b = off_in[kk];
+    if ((uint32_t)p < b || (uint32_t)p >= off_in[kk + 1]) return;   // never for a sorted set
+    const uint32_t rank = (uint32_t)p - b;
+    if (rank >= (uint32_t)cap) return;
+    const uint32_t o = off_out[kk] + rank;
+    pos_out[o] = x;
+    vel_out[o] = vel[p];
 }
 
 // ------------------------------------------------------------------ scan
@@ -260,9 +279,10 @@ static int finish_sort(Sim *s, long long ncells, bool /*was_in_order*/) {
         GFS_LAUNCH_CHECK();
         int rc = exclusive_scan_u32(ctx, count, count, ncells + 1, s->scan_tmp.as<uint32_t>(), st);
         if (rc) return rc;
-        k_cap_copy<<<grid_blocks(ncells, T), T, 0, st>>>(s->pos.as<float4>(), s->vel.as<float4>(),
-                                                         offset, count, ncells, s->pos_alt.as<float4>(),
-                                                         s->vel_alt.as<float4>(), num);
+        const long long n = host_num[0];
+        k_cap_copy<<<grid_blocks(n > 0 ? n : 1, T), T, 0, st>>>(
+            s->pos.as<float4>(), s->vel.as<float4>(), offset, count, ncells, n, s->g.c, 1.0 / s->g.dx, s->inv_dx_f,
+            s->dx_pow2 ? 1 : 0, cap, s->pos_alt.as<float4>(), s->vel_alt.as<float4>(), num);
         ctx->launches++;
         GFS_LAUNCH_CHECK();
         std::swap(s->pos.p, s->pos_alt.p);
