@@ -246,6 +246,8 @@ static int sim_init(Sim *s, Ctx *ctx, int ni, int nj, int nk, double dx, int64_t
     int rc = 0;
     rc |= s->mat.alloc((size_t)c.size);
     rc |= s->layer.alloc((size_t)c.size);
+    rc |= s->lcells.alloc((size_t)c.size * sizeof(uint32_t));
+    rc |= s->lcnt.alloc((size_t)(GFS_MAX_LAYERS + 1) * sizeof(uint32_t));
     for (int d = 0; d < 3; d++) {
         const GridDim &f = s->g.f[d];
         rc |= s->mac[d].alloc((size_t)f.size * sizeof(float));

@@ -133,6 +133,7 @@ struct Sim {
     DevMem mac[3], saved[3];     // float padded face grids
     DevMem sval[3], smask[3];    // splat value / is-set mask
     DevMem layer;                // int8 padded cell grid
+    DevMem lcells, lcnt;         // cells of each extrapolation layer (storage indices, layer by layer); counts
     DevMem pos, vel, pos_alt, vel_alt;   // float4 x capacity
     DevMem key, slot;            // uint32 x capacity
     DevMem count, offset, scan_tmp;      // uint32 x (ncells + 1), scan block sums
@@ -203,6 +204,7 @@ int splat_points(Ctx *ctx, const float *d_pts, const float *d_vals, long long n,
                  bool thr_set, float thr);
 
 // ---- extrapolate.cu
+#define GFS_MAX_LAYERS 126       // layers fit in the int8 layer grid
 int build_layers(Sim *s, int num_layers);
 int extrapolate_field(Sim *s, float *const f[3], int num_layers, bool reset);
 
