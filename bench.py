@@ -88,7 +88,7 @@ BYTES = {
 # two forward / backward pairs of this bench's mixed run.  A sweep streams every
 # plane of each block that holds fluid (134 of the 256 blocks here), air and
 # padding slots included.
-TRAFFIC = {"mic0_forward": 97.1e6, "mic0_backward": 143.2e6}
+TRAFFIC = {"mic0_forward": 96.8e6, "mic0_backward": 141.4e6}
 
 # FP32 work of the fused PIC/FLIP + RK4 pass per particle: 5 Catmull-Rom samples
 # (MAC at the particle and the 3 later RK4 stages, saved field at the particle) x
