@@ -1545,26 +1545,14 @@ __global__ void __launch_bounds__(WT_THREADS, 1) k_tri_warp(SweepArgs<float> A) 
                 if (lane == 0) atomicOr(&A.ctrl->err, GFS_DEV_ERR_TIMEOUT);
                 break;
             }
-            if (s < end) {
-                if (!inflight) {
-                    // ring slot s & (RX_R-1) is free once the compute warp has read step s - RX_R
-                    if (s < max(ld_volatile_s32(&rx.cons), lo) + RX_R - RX_CB) {
-                        w = ld_cg_u64(src + (long long)s * XS);
-                        inflight = true;
-                    } else {
-                        __nanosleep(32);
-                    }
-                } else if ((unsigned)(w >> 32) == wtag) {
+            // a round: take the word that arrived, publish, and only then issue the next
+            // reads -- a fence behind a read still in flight would wait for its round trip
+            if (s < end && inflight) {
+                if ((unsigned)(w >> 32) == wtag) {
                     rx.val[s & (RX_R - 1)][lane] = __uint_as_float((unsigned)(w & 0xFFFFFFFFull));
                     s += RX_NR;
-                    inflight = false;
-                    if (s < end && s < max(ld_volatile_s32(&rx.cons), lo) + RX_R - RX_CB) {
-                        w = ld_cg_u64(src + (long long)s * XS);
-                        inflight = true;
-                    }
-                } else {
-                    w = ld_cg_u64(src + (long long)s * XS);
                 }
+                inflight = false;   // arrived (taken or stale): read again below
             }
             const int m = __reduce_min_sync(FULL, s < end ? s : S);
             if (m > pub) {
@@ -1574,6 +1562,15 @@ __global__ void __launch_bounds__(WT_THREADS, 1) k_tri_warp(SweepArgs<float> A) 
                     st_volatile_s32(&rx.prog[r], m);
                 }
                 pub = m;
+            }
+            if (s < end) {
+                // ring slot s & (RX_R-1) is free once the compute warp has read step s - RX_R
+                if (s < max(ld_volatile_s32(&rx.cons), lo) + RX_R - RX_CB) {
+                    w = ld_cg_u64(src + (long long)s * XS);
+                    inflight = true;
+                } else {
+                    __nanosleep(32);
+                }
             }
         }
         __syncwarp();
