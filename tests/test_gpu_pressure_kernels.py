@@ -135,6 +135,23 @@ def test_warp_kernel_against_block_kernel_and_oracle(kernel_ctx, oracle_lib, sys
     assert np.array_equal(qw, qb) and tw.iterations == tb.iterations
 
 
+@pytest.mark.parametrize("dims", [(3, 40, 36), (5, 17, 33), (40, 18, 18)])
+def test_warp_kernel_shapes(kernel_ctx, oracle_lib, dims):
+    """The one-warp kernel on grids whose i extent is shorter than a copy group (3 and
+    5 planes: 33 and 35 wavefront steps, the last copy group partial and the last
+    progress check reaching past the end) or whose j / k extents leave partial pencil
+    blocks: the MIXED bars against an FP64 solve to 1e-12."""
+    O = oracle_lib
+    sc, mat, uvw = _system(O, dims=dims, seed=4)
+    exact, _, _ = O.pressure_solve(sc.dims, sc.dx, 20.0, sc.dt, mat, *uvw, tol=1e-12, max_iters=4000)
+    kernel_ctx.set_sweep_kernel(SWEEP_WARP)
+    p, solver = _solve(kernel_ctx, sc, mat, uvw, PRECISION_MIXED)
+    assert kernel_ctx.last_sweep_kernel() == SWEEP_WARP
+    assert O.pressure_residual(sc.dims, sc.dx, 20.0, sc.dt, mat, *uvw, p) < 1e-6
+    if np.abs(exact).max() > 0:
+        assert np.abs(p - exact).max() / np.abs(exact).max() < 1e-5
+
+
 def test_invalid_kernel_is_rejected(kernel_ctx):
     with pytest.raises(GFSError):
         kernel_ctx.set_sweep_kernel(7)
