@@ -917,7 +917,9 @@ def main(args):
         adjoint = adjoint_bench(ctx)
     if r == 0 and set(forms) != {"plain", "mixed"}:
         # partial run (profiling): report the timed forms only
-        print(json.dumps({k: {"ms_per_step": v["t"] / args.steps * 1e3, "gpu_launches": int(v["launches"])}
+        print(json.dumps({k: {"ms_per_step": v["t"] / args.steps * 1e3, "gpu_launches": int(v["launches"]),
+                              "ms_per_stage": {s: round(t[0] / args.steps, 3) for s, t in
+                                               sorted(v["prof"].items(), key=lambda kv: -kv[1][0]) if t[0] > 0}}
                           for k, v in results.items()}), flush=True)
     elif r == 0:
         mixed, plain = results["mixed"], results["plain"]

@@ -10,7 +10,8 @@
 // The tricubic sample is MACVelocityField::evaluateVelocityAtPosition
 // (macvelocityfield.cpp:350-559): Catmull-Rom over a 4x4x4 stencil per
 // component, evaluated here in FP32 in separable form, reading the padded face
-// grids through the read-only path with no bounds checks (the zero halo is the
+// grids (the four MAC samples: their row quads, one 16-byte load per stencil row)
+// through the read-only path with no bounds checks (the zero halo is the
 // reference's out-of-range value).  With a power-of-two dx the stencil index
 // and the fractional offsets are formed exactly as the reference's doubles.
 #include <mutex>
@@ -20,10 +21,37 @@
 
 namespace gfs {
 
+// Row quads of a face grid: q[x] = (g[x], g[x+1], g[x+2], g[x+3]) at every
+// storage index x, 0 past the grid's end.  A Catmull-Rom stencil row of four x
+// taps is then one aligned 16-byte load (row_taps) where the grid itself needs
+// four 4-byte loads.  The four MAC samples of G2P (vnew and the RK4 stages) read
+// the quads of the MAC field; the one sample of the saved field reads its taps
+// directly (quads of both fields measured slower: their build costs more than the
+// one sample saves).  blockIdx.y picks the grid.
+struct QuadJob {
+    const float *src[3];
+    float4 *dst[3];
+    long long n[3];
+};
+
+__global__ void __launch_bounds__(256) k_row_quads(QuadJob J) {
+    const float *__restrict__ g = J.src[blockIdx.y];
+    float4 *__restrict__ q = J.dst[blockIdx.y];
+    const long long n = J.n[blockIdx.y];
+    for (long long x = blockIdx.x * 256ll + threadIdx.x; x < n; x += (long long)gridDim.x * 256) {
+        float4 t;
+        t.x = g[x];
+        t.y = x + 1 < n ? g[x + 1] : 0.f;
+        t.z = x + 2 < n ? g[x + 2] : 0.f;
+        t.w = x + 3 < n ? g[x + 3] : 0.f;
+        q[x] = t;
+    }
+}
+
 __global__ void __launch_bounds__(128) k_g2p_advect(AdvArgs A, float4 *__restrict__ pos, float4 *__restrict__ vel,
                                                     const uint32_t *__restrict__ num, long long nbound,
-                                                    const float *__restrict__ mu, const float *__restrict__ mv,
-                                                    const float *__restrict__ mw, const float *__restrict__ su,
+                                                    const float4 *__restrict__ mu, const float4 *__restrict__ mv,
+                                                    const float4 *__restrict__ mw, const float *__restrict__ su,
                                                     const float *__restrict__ sv, const float *__restrict__ sw,
                                                     const uint8_t *__restrict__ mat) {
     long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -93,9 +121,18 @@ int g2p_advect(Sim *s, double dt) {
     AdvArgs A = make_adv(s->g, dt, s->params.ratio_pic);
     long long nb = s->n_bound;
     if (nb == 0) return GFS_OK;
+    QuadJob J;
+    for (int d = 0; d < 3; d++) {
+        J.src[d] = s->mac[d].as<float>();
+        J.dst[d] = s->quad[d].as<float4>();
+        J.n[d] = s->g.f[d].size;
+    }
+    k_row_quads<<<dim3((unsigned)ctx->num_sms * 4, 3), 256, 0, ctx->stream>>>(J);
+    ctx->launches++;
+    GFS_LAUNCH_CHECK();
     k_g2p_advect<<<grid_blocks(nb, 128), 128, 0, ctx->stream>>>(
-        A, s->pos.as<float4>(), s->vel.as<float4>(), s->num.as<uint32_t>(), nb, s->mac[0].as<float>(),
-        s->mac[1].as<float>(), s->mac[2].as<float>(), s->saved[0].as<float>(), s->saved[1].as<float>(),
+        A, s->pos.as<float4>(), s->vel.as<float4>(), s->num.as<uint32_t>(), nb, s->quad[0].as<float4>(),
+        s->quad[1].as<float4>(), s->quad[2].as<float4>(), s->saved[0].as<float>(), s->saved[1].as<float>(),
         s->saved[2].as<float>(), s->mat.as<uint8_t>());
     ctx->launches++;
     GFS_LAUNCH_CHECK();

@@ -252,6 +252,7 @@ static int sim_init(Sim *s, Ctx *ctx, int ni, int nj, int nk, double dx, int64_t
         const GridDim &f = s->g.f[d];
         rc |= s->mac[d].alloc((size_t)f.size * sizeof(float));
         rc |= s->saved[d].alloc((size_t)f.size * sizeof(float));
+        rc |= s->quad[d].alloc((size_t)f.size * sizeof(float4));
         rc |= s->sval[d].alloc((size_t)f.size * sizeof(float));
         rc |= s->smask[d].alloc((size_t)f.size);
     }

@@ -131,6 +131,7 @@ struct Sim {
 
     DevMem mat;                  // uint8 padded cell grid
     DevMem mac[3], saved[3];     // float padded face grids
+    DevMem quad[3];              // float4 row quads of mac, rebuilt for each G2P pass
     DevMem sval[3], smask[3];    // splat value / is-set mask
     DevMem layer;                // int8 padded cell grid
     DevMem lcells, lcnt;         // cells of each extrapolation layer (storage indices, layer by layer); counts

@@ -23,8 +23,28 @@ struct AdvArgs {
     float a_pic, b_flip;
 };
 
-__device__ __forceinline__ float interp_component(const float *__restrict__ g, const GridDim &f, float X,
-                                                  float Y, float Z) {
+// The four x taps g[at .. at+3] of one stencil row: four 4-byte loads from a face
+// grid, or one aligned 16-byte load from its row quads (k_row_quads in advect.cu:
+// quad x holds the grid's values at storage indices x .. x+3).
+__device__ __forceinline__ float4 row_taps(const float *__restrict__ g, long long at) {
+    return make_float4(__ldg(g + at), __ldg(g + at + 1), __ldg(g + at + 2), __ldg(g + at + 3));
+}
+__device__ __forceinline__ float4 row_taps(const float4 *__restrict__ q, long long at) { return __ldg(q + at); }
+
+// One Catmull-Rom row w0 v0 + w1 v1 + w2 v2 + w3 v3: the product w1 v1 rounded,
+// then w0 v0, w2 v2 and w3 v3 fused into the running sum in that order.  The order
+// is spelled out so that every sampler below (the scalar and the row-quad forms,
+// and the gradient form the adjoint recomputes the forward with) rounds the same
+// way; it is the order the substep parity tests against the oracle hold with.
+__device__ __forceinline__ float cr_row(const float w[4], float4 t) {
+    return __fmaf_rn(w[3], t.w, __fmaf_rn(w[2], t.z, __fmaf_rn(w[0], t.x, __fmul_rn(w[1], t.y))));
+}
+// a += w r, fused
+#define CR_ACC(a, w, r) ((a) = __fmaf_rn((w), (r), (a)))
+
+template <class G>
+__device__ __forceinline__ float interp_component(const G *__restrict__ g, const GridDim &f, float X, float Y,
+                                                  float Z) {
     float fi = floorf(X), fj = floorf(Y), fk = floorf(Z);
     int i = (int)fi, j = (int)fj, k = (int)fk;
     float wx[4], wy[4], wz[4];
@@ -32,26 +52,23 @@ __device__ __forceinline__ float interp_component(const float *__restrict__ g, c
     catmull_rom_weights(Y - fj, wy);
     catmull_rom_weights(Z - fk, wz);
     const long long sy = f.sx, sz = (long long)f.sx * f.sy;
-    const float *base = g + f.at(i - 1, j - 1, k - 1);
+    const long long base = f.at(i - 1, j - 1, k - 1);
     float acc = 0.0f;
 #pragma unroll
     for (int c = 0; c < 4; c++) {
         float accb = 0.0f;
 #pragma unroll
-        for (int b = 0; b < 4; b++) {
-            const float *row = base + b * sy + c * sz;
-            float r = wx[0] * __ldg(row) + wx[1] * __ldg(row + 1) + wx[2] * __ldg(row + 2) + wx[3] * __ldg(row + 3);
-            accb += wy[b] * r;
-        }
-        acc += wz[c] * accb;
+        for (int b = 0; b < 4; b++) CR_ACC(accb, wy[b], cr_row(wx, row_taps(g, base + b * sy + c * sz)));
+        CR_ACC(acc, wz[c], accb);
     }
     return acc;
 }
 
-// MACVelocityField::evaluateVelocityAtPosition: zero outside [0, n*dx).
-__device__ __forceinline__ float3 eval_velocity(const AdvArgs &A, const float *__restrict__ u,
-                                                const float *__restrict__ v, const float *__restrict__ w,
-                                                float x, float y, float z) {
+// MACVelocityField::evaluateVelocityAtPosition: zero outside [0, n*dx).  G is
+// float (the face grids) or float4 (their row quads).
+template <class G>
+__device__ __forceinline__ float3 eval_velocity(const AdvArgs &A, const G *__restrict__ u, const G *__restrict__ v,
+                                                const G *__restrict__ w, float x, float y, float z) {
     if (!(x >= 0.f && y >= 0.f && z >= 0.f && x < A.bound[0] && y < A.bound[1] && z < A.bound[2]))
         return make_float3(0.f, 0.f, 0.f);
     float X, Y, Z;
@@ -234,18 +251,17 @@ __device__ __forceinline__ float interp_component_grad(const float *__restrict__
         float ab = 0.f, abx = 0.f, aby = 0.f;
 #pragma unroll
         for (int b = 0; b < 4; b++) {
-            const float *row = base + b * sy + c * sz;
-            float v0 = __ldg(row), v1 = __ldg(row + 1), v2 = __ldg(row + 2), v3 = __ldg(row + 3);
-            float r = wx[0] * v0 + wx[1] * v1 + wx[2] * v2 + wx[3] * v3;
-            float rx = dx_[0] * v0 + dx_[1] * v1 + dx_[2] * v2 + dx_[3] * v3;
-            ab += wy[b] * r;
-            abx += wy[b] * rx;
-            aby += dy_[b] * r;
+            const float4 t = row_taps(base, (long long)(b * sy + c * sz));
+            const float r = cr_row(wx, t);
+            const float rx = cr_row(dx_, t);
+            CR_ACC(ab, wy[b], r);
+            CR_ACC(abx, wy[b], rx);
+            CR_ACC(aby, dy_[b], r);
         }
-        acc += wz[c] * ab;
-        gx += wz[c] * abx;
-        gy += wz[c] * aby;
-        gz += dz_[c] * ab;
+        CR_ACC(acc, wz[c], ab);
+        CR_ACC(gx, wz[c], abx);
+        CR_ACC(gy, wz[c], aby);
+        CR_ACC(gz, dz_[c], ab);
     }
     grad[0] = gx;
     grad[1] = gy;

@@ -2114,23 +2114,41 @@ __global__ void __launch_bounds__(RED_THREADS) k_mixed_prepare(Skew K, const uin
     }
 }
 
+// The per-update kernels of the MIXED form below walk the solve's FP32 strip
+// list (8 slots per strip, the list the inner PCG builds); each FP32 strip is two
+// 4-slot FP64 strips of the FP64 vectors.  Slots outside the listed strips hold no
+// fluid, and the vectors' non-fluid slots keep the 0 that k_mixed_prepare wrote
+// at the start of the solve (the inner PCG stores fluid slots only).
+
 // MIXED, reliable update: the inner FP32 CG goes on with the true residual.
 // r32 = r64 (the FP64 residual of the corrected p64), e32 = 0, and the search
 // direction s32 and sigma are kept, so the Krylov information of the earlier
 // inner iterations is not thrown away.  The pending preconditioner apply of the
 // iteration that met the inner threshold completes that iteration, so the
 // iteration counter restarts at -1 (that apply brings it to 0).
-__global__ void __launch_bounds__(RED_THREADS) k_mixed_reliable(Skew K, const uint8_t *__restrict__ fsk,
-                                                                const double *__restrict__ r64,
+__global__ void __launch_bounds__(RED_THREADS) k_mixed_reliable(VecArgs<float> A, const double *__restrict__ r64,
                                                                 float *__restrict__ r32, float *__restrict__ e32,
-                                                                PsCtrl *ctrl, double eta) {
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < K.size;
-         q += (long long)gridDim.x * blockDim.x) {
-        bool f = fsk[q] & GFS_PF_FLUID;
-        r32[q] = f ? (float)r64[q] : 0.0f;
-        e32[q] = 0.0f;
+                                                                double eta) {
+    for (StripWalk sw(A.slist, A.snum); sw.more();) {
+        const long long q0 = (long long)sw.take() * Strip<float>::W;
+        StripFlags<float> f;
+        f.load(A.fsk, q0);
+        double lo[4], hi[4];
+        load_strip<double>(lo, r64 + q0);
+        load_strip<double>(hi, r64 + q0 + 4);
+        float rv[8];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            rv[e] = f.fluid(e) ? (float)lo[e] : 0.0f;
+            rv[e + 4] = f.fluid(e + 4) ? (float)hi[e] : 0.0f;
+        }
+        *reinterpret_cast<float4 *>(r32 + q0) = make_float4(rv[0], rv[1], rv[2], rv[3]);
+        *reinterpret_cast<float4 *>(r32 + q0 + 4) = make_float4(rv[4], rv[5], rv[6], rv[7]);
+        *reinterpret_cast<float4 *>(e32 + q0) = make_float4(0.f, 0.f, 0.f, 0.f);
+        *reinterpret_cast<float4 *>(e32 + q0 + 4) = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
+        PsCtrl *ctrl = A.ctrl;
         double m = ctrl->maxr64;
         ctrl->inner_tol = fmax(eta * m, 0.25 * ctrl->tol);
         ctrl->done = 0;
@@ -2140,30 +2158,56 @@ __global__ void __launch_bounds__(RED_THREADS) k_mixed_reliable(Skew K, const ui
 }
 
 // MIXED: p64 += e32 (outer refinement)
-__global__ void __launch_bounds__(RED_THREADS) k_mixed_correct(Skew K, const uint8_t *__restrict__ fsk,
-                                                               double *__restrict__ p64,
+__global__ void __launch_bounds__(RED_THREADS) k_mixed_correct(VecArgs<float> A, double *__restrict__ p64,
                                                                const float *__restrict__ e32) {
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < K.size;
-         q += (long long)gridDim.x * blockDim.x)
-        if (fsk[q] & GFS_PF_FLUID) p64[q] += (double)e32[q];
+    for (StripWalk sw(A.slist, A.snum); sw.more();) {
+        const long long q0 = (long long)sw.take() * Strip<float>::W;
+        StripFlags<float> f;
+        f.load(A.fsk, q0);
+        float ev[8];
+        load_strip<float>(ev, e32 + q0);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            StripFlags<double> fh;
+            fh.w[0] = f.w[h];
+            double pv[4];
+            load_strip<double>(pv, p64 + q0 + 4 * h);
+#pragma unroll
+            for (int e = 0; e < 4; e++) pv[e] += (double)ev[4 * h + e];
+            store_strip_fluid<double>(p64 + q0 + 4 * h, pv, fh);
+        }
+    }
 }
 
-// MIXED: r64 = b - A p64 in FP64 and max|r64|
+// MIXED: r64 = b - A p64 in FP64 and max|r64|.  A carries the FP32 strip list.
 __global__ void __launch_bounds__(RED_THREADS) k_residual64(VecArgs<double> A, const double *__restrict__ b,
                                                             const double *__restrict__ p,
                                                             double *__restrict__ r) {
     using Op = Ar<double>;
+    constexpr int W = Strip<double>::W;
     const Skew &K = A.K;
     double mx = 0.0;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < K.size;
-         q += (long long)gridDim.x * blockDim.x) {
-        uint8_t fl = A.fsk[q];
-        if (!(fl & GFS_PF_FLUID)) continue;
-        double val = Op::mul(neighbour_sum<double>(K, p, q), A.negscale);
-        val = Op::add(val, Op::mul(Op::mul((double)(fl >> 1), A.scale), p[q]));
-        double rv = b[q] - val;
-        r[q] = rv;
-        mx = fmax(mx, fabs(rv));
+    for (StripWalk sw(A.slist, A.snum); sw.more();) {
+        const unsigned u = sw.take() * 2u;   // the FP32 strip's two FP64 strips
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const StripPos P = strip_pos<double>(K, u + (unsigned)h);
+            StripFlags<double> f;
+            f.load(A.fsk, P.q0);
+            double xc[W], bv[W], val[W];
+            load_strip<double>(xc, p + P.q0);
+            load_strip<double>(bv, b + P.q0);
+            neighbour_sum_strip<double>(K, p, P, val);
+#pragma unroll
+            for (int e = 0; e < W; e++) {
+                const unsigned fl = f.at(e);
+                double v = Op::mul(val[e], A.negscale);
+                v = Op::add(v, Op::mul(Op::mul((double)(fl >> 1), A.scale), xc[e]));
+                val[e] = bv[e] - v;
+                if (fl & GFS_PF_FLUID) mx = fmax(mx, fabs(val[e]));
+            }
+            store_strip_fluid<double>(r + P.q0, val, f);
+        }
     }
     double part = block_reduce<1>(mx);
     double res;
@@ -2523,8 +2567,7 @@ static int run_cg(Ctx *ctx, PressureWs &ws, const Skew &K, double scale, bool mi
                     k_mixed_prepare<<<nb, RED_THREADS, 0, st>>>(K, ws.fsk.as<uint8_t>(), ws.r.as<double>(), r32,
                                                                e32, s32, C, eta);
                 else
-                    k_mixed_reliable<<<nb, RED_THREADS, 0, st>>>(K, ws.fsk.as<uint8_t>(), ws.r.as<double>(), r32,
-                                                                e32, C, eta);
+                    k_mixed_reliable<<<nb, RED_THREADS, 0, st>>>(V32, ws.r.as<double>(), r32, e32, eta);
             }
             ctx->launches++;
             // the inner cap is what is left of the total budget
@@ -2559,7 +2602,7 @@ static int run_cg(Ctx *ctx, PressureWs &ws, const Skew &K, double scale, bool mi
             sweeps += 1 + h.iter;
             {
                 ProfScope prof(ctx, KC_MIXED_AUX);
-                k_mixed_correct<<<nb, RED_THREADS, 0, st>>>(K, ws.fsk.as<uint8_t>(), ws.psk.as<double>(), e32);
+                k_mixed_correct<<<nb, RED_THREADS, 0, st>>>(V32, ws.psk.as<double>(), e32);
                 k_residual64<<<nb, RED_THREADS, 0, st>>>(V64, ws.bsk.as<double>(), ws.psk.as<double>(),
                                                           ws.r.as<double>());
             }
