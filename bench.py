@@ -815,6 +815,7 @@ def main(args):
     import torch
     import torch.distributed as dist
     from gridfluidsim3d_gb300 import PRECISION_MIXED, PRECISION_PLAIN, Context, FluidSimulation, _lib
+    from gridfluidsim3d_gb300 import SWEEP_BLOCK, SWEEP_WARP
     from gridfluidsim3d_gb300 import build as gb
 
     r, world, lr = rank_info()
@@ -830,6 +831,8 @@ def main(args):
     _lib.load()
     sc = make_scene()
     ctx = Context(lr)
+    if args.sweep != "auto":
+        ctx.set_sweep_kernel({"block": SWEEP_BLOCK, "warp": SWEEP_WARP}[args.sweep])
     # room for the particles the fluid-source leg adds (an inflow sphere of radius 12 cells)
     sim = FluidSimulation(*sc.dims, sc.dx, max_particles=sc.num_particles + 1_000_000, ctx=ctx)
     dt = sc.dt
@@ -1048,6 +1051,8 @@ def parse():
     ap.add_argument("--no-check", action="store_true", help="skip the per-step FP64 pressure check")
     ap.add_argument("--no-savestate", action="store_true", help="skip the savestate write/read leg")
     ap.add_argument("--no-configs", action="store_true", help="skip the 64^3 / 128^3 forward configurations")
+    ap.add_argument("--sweep", choices=["auto", "block", "warp"], default="auto",
+                    help="the triangular solves' kernel (auto: the library's choice)")
     ap.add_argument("--grid", type=int, default=256,
                     help="grid size of the scene (the workload is 256; smaller grids are for small profiler captures)")
     a = ap.parse_args()

@@ -566,12 +566,19 @@ int gfs_ctx_create(int device, gfs_ctx **out) {
     return GFS_OK;
 }
 
-int gfs_ctx_destroy(gfs_ctx *ctx) {
-    if (!ctx) return GFS_OK;
+static void ctx_free(gfs_ctx *ctx) {
     cudaSetDevice(ctx->c.device);
     cudaStreamSynchronize(ctx->c.stream);
     cudaStreamDestroy(ctx->c.stream);
     delete ctx;
+}
+
+int gfs_ctx_destroy(gfs_ctx *ctx) {
+    if (!ctx) return GFS_OK;
+    cudaSetDevice(ctx->c.device);
+    cudaStreamSynchronize(ctx->c.stream);
+    ctx->closed.store(true);
+    if (ctx->sims.load() == 0) ctx_free(ctx);   // else the last simulation destroyed frees it
     return GFS_OK;
 }
 
@@ -693,6 +700,8 @@ int gfs_sim_create(gfs_ctx *ctx, int ni, int nj, int nk, double dx, int64_t max_
         set_error(GFS_ERR_NOMEM, "host allocation failed");
         return GFS_ERR_NOMEM;
     }
+    s->owner = ctx;
+    ctx->sims.fetch_add(1);
     int rc = sim_init(&s->s, &ctx->c, ni, nj, nk, dx, max_particles);
     if (rc) {
         gfs_sim_destroy(s);
@@ -710,7 +719,9 @@ int gfs_sim_destroy(gfs_sim *sim) {
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->evp0) cudaEventDestroy(s->evp0);
     if (s->evp1) cudaEventDestroy(s->evp1);
+    gfs_ctx *owner = sim->owner;
     delete sim;
+    if (owner && owner->sims.fetch_sub(1) == 1 && owner->closed.load()) ctx_free(owner);
     return GFS_OK;
 }
 

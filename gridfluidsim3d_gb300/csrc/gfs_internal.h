@@ -1,6 +1,8 @@
 // gfs_internal.h -- host-side structures shared by the libgfs translation units.
 #pragma once
 
+#include <atomic>
+
 #include <cstdarg>
 #include <cstdint>
 #include <vector>
@@ -237,10 +239,15 @@ int interpolate_points(Ctx *ctx, const Grids &g, float *const mac[3], const floa
 
 }  // namespace gfs
 
+// A context stays allocated while simulations built on it are alive: destroying
+// it only marks it closed, and the last simulation destroyed frees it.
 struct gfs_ctx {
     gfs::Ctx c;
+    std::atomic<int> sims{0};
+    std::atomic<bool> closed{false};
 };
 
 struct gfs_sim {
     gfs::Sim s;
+    gfs_ctx *owner = nullptr;
 };

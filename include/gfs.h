@@ -61,6 +61,9 @@ const char *gfs_version(void);
    (clscalarfield.cpp:33-66) and ParticleAdvector::initialize
    (particleadvector.cpp:33-63). */
 int gfs_ctx_create(int device, gfs_ctx **out);
+/* Closes the context.  Simulations created on it stay usable until they are
+   destroyed; the last of them frees the context (so the two may be destroyed in
+   either order, as a garbage collector may do). */
 int gfs_ctx_destroy(gfs_ctx *ctx);
 /* Wait for all work queued on the context's stream. */
 int gfs_ctx_synchronize(gfs_ctx *ctx);

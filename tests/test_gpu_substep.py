@@ -214,3 +214,28 @@ def test_g2p_matches_standalone_sampler(gpu_ctx, speed):
         disp = np.abs(want - p0).max(axis=1) / sc.dx
         assert (disp > 2.0).sum() > 100
     sim.close()
+
+
+def test_context_closed_before_its_simulation():
+    """A garbage collector may finalise a context before a simulation built on it:
+    the C context then stays allocated until the simulation is destroyed, and the
+    simulation keeps stepping (the same state as on a context that stays open)."""
+    import ctypes
+    from gridfluidsim3d_gb300 import Context, _lib
+    sc = scenes.random_box(dims=(20, 18, 16), seed=4)
+    out = []
+    for early_close in (False, True):
+        ctx = Context(0)
+        sim = FluidSimulation(*sc.dims, sc.dx, max_particles=sc.num_particles, ctx=ctx)
+        sim.set_material_grid(sc.mat)
+        sim.set_marker_particles(sc.pos, sc.vel, sc.ids)
+        sim.update(sc.dt)
+        if early_close:
+            _lib.lib().gfs_ctx_destroy(ctx.handle)   # as a finaliser running first would
+            ctx._h = ctypes.c_void_p()
+        sim.update(sc.dt)
+        out.append(sim.get_marker_particles())
+        sim.close()
+        ctx.close()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
