@@ -313,9 +313,24 @@ __device__ __forceinline__ float3 eval_velocity_jac(const AdvArgs &A, const floa
 // not depend on the order in which the particles arrive.  |weight| <= 1 for
 // Catmull-Rom, so |term| <= |c| * scale; the caller picks scale (a power of two)
 // so that no node sum can leave the int64 range.
+// round(w) to the nearest int64, ties to even, in FP32 and integer arithmetic (|w| < 2^62):
+// below 2^23 the 32-bit conversion, above it w is an integer whose 24-bit significand
+// is shifted into place.
+__device__ __forceinline__ long long fix_round(float w) {
+    if (fabsf(w) < 8388608.0f) return (long long)__float2int_rn(w);
+    const unsigned bits = __float_as_uint(w);
+    const long long mag = (long long)((bits & 0x7FFFFFu) | 0x800000u) << (int)(((bits >> 23) & 0xFFu) - 150u);
+    return (bits >> 31) ? -mag : mag;
+}
+
 __device__ __forceinline__ void scatter_component_fixed(unsigned long long *__restrict__ g, const GridDim &f, float X,
                                                         float Y, float Z, float c, double scale) {
     if (c == 0.0f || scale == 0.0) return;
+    // The term is round((double)(weight * c) * scale) with scale a power of two.  Within
+    // float range the scaling is exact in FP32 too (a result below the normal range rounds
+    // to 0 either way), so the term is formed without FP64, whose rate on GB300 is a
+    // small fraction of FP32's; outside that range the FP64 form runs.
+    const float scalef = (scale >= 0x1p-126 && scale <= 0x1p126) ? (float)scale : 0.0f;
     float fi = floorf(X), fj = floorf(Y), fk = floorf(Z);
     int i = (int)fi, j = (int)fj, k = (int)fk;
     float wx[4], wy[4], wz[4];
@@ -332,7 +347,8 @@ __device__ __forceinline__ void scatter_component_fixed(unsigned long long *__re
             unsigned long long *row = base + b * sy + cc * sz;
 #pragma unroll
             for (int a = 0; a < 4; a++) {
-                long long t = __double2ll_rn((double)(wx[a] * wbc) * scale);
+                const float w = wx[a] * wbc;
+                const long long t = scalef != 0.0f ? fix_round(w * scalef) : __double2ll_rn((double)w * scale);
                 if (t) atomicAdd(row + a, (unsigned long long)t);
             }
         }
