@@ -106,6 +106,7 @@ struct PressureWs {
     DevMem flags, b, p;          // padded cell layout: uint8, FP64, FP64 (the solution)
     DevMem fsk;                  // skewed flags
     DevMem bsk, psk, r, z, s, As, q, precon;        // FP64, skewed
+    DevMem mpc;                  // FP64 negscale * precon (the FP64 block solves read it)
     DevMem r32, z32, s32, As32, q32, e32, precon32; // FP32 (mixed), skewed
     DevMem partials;             // double per block
     DevMem ctrl;                 // PsCtrl

@@ -288,6 +288,7 @@ struct SweepArgs {
     T *out;                  // FWD: q, BWD: z, PRECON: precon (double)
     const T *precon;         // FWD/BWD
     const T *rdot;           // BWD: r, for dot(z, r)
+    const T *mpc;            // FWD/BWD in FP64: negscale * precon, precomputed (k_tri)
     float *out32;            // PRECON: float copy of precon (MIXED)
     T negscale;
     double scale, dnegscale;
@@ -833,7 +834,11 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
     constexpr long long PS = bwd ? -(long long)SPLANE : (long long)SPLANE;
     constexpr long long XP = (long long)XCH_PER_PLANE * X::W;
     constexpr long long XS = bwd ? -XP : XP;
-    constexpr int NARR = bwd ? 3 : 2;
+    // FP64 solves read negscale * precon (one FP64 multiply per cell fewer: GB300's FP64
+    // rate bounds them) from ring array IM; FP32 solves form it
+    constexpr bool PM = sizeof(T) == 8;
+    constexpr int IM = bwd ? 3 : 2;
+    constexpr int NARR = (bwd ? 3 : 2) + (PM ? 1 : 0);
     __shared__ T xb[2][SBK][SBJ];
     __shared__ __align__(16) T ring[NARR][P][SPLANE];
     __shared__ unsigned sh_ticket, sh_epoch;
@@ -903,8 +908,8 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
     const int cpi = tid - NCP;
     const bool copier = cpi >= 0 && cpi < NCP;
     const long long qp = K.base(bj, bk) + (bwd ? (long long)(S - 1) * SPLANE : 0) + (long long)(copier ? cpi : 0) * E;
-    const T *ca = A.in + qp, *cb = A.precon + qp, *cc = (bwd ? A.rdot : A.in) + qp;
-    const T *fa = ca + P * PS, *fb = cb + P * PS, *fc = cc + P * PS;   // the first refill: step P
+    const T *ca = A.in + qp, *cb = A.precon + qp, *cc = (bwd ? A.rdot : A.in) + qp, *cm = (PM ? A.mpc : A.in) + qp;
+    const T *fa = ca + P * PS, *fb = cb + P * PS, *fc = cc + P * PS, *fm = cm + P * PS;   // the first refill: step P
     T *po = A.out + q0;
     unsigned long long *xbuf = A.xch;
     unsigned long long *pxj_out = xbuf + (long long)(bk * K.nbj + bj) * xblock + (bwd ? (long long)(S - 1) * XP : 0) +
@@ -926,7 +931,8 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
         if (copier && u < S && live) {
             cp_async<16>(&ring[0][u][cpi * E], ca + u * PS, true);
             cp_async<16>(&ring[1][u][cpi * E], cb + u * PS, true);
-            if (bwd) cp_async<16>(&ring[NARR - 1][u][cpi * E], cc + u * PS, true);
+            if (bwd) cp_async<16>(&ring[2][u][cpi * E], cc + u * PS, true);
+            if (PM) cp_async<16>(&ring[IM][u][cpi * E], cm + u * PS, true);
         }
         cp_async_commit();
     }
@@ -947,11 +953,13 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
                 if (st - 1 + P < S) {
                     cp_async<16>(&ring[0][(u + P - 1) % P][cpi * E], fa, true);
                     cp_async<16>(&ring[1][(u + P - 1) % P][cpi * E], fb, true);
-                    if (bwd) cp_async<16>(&ring[NARR - 1][(u + P - 1) % P][cpi * E], fc, true);
+                    if (bwd) cp_async<16>(&ring[2][(u + P - 1) % P][cpi * E], fc, true);
+                    if (PM) cp_async<16>(&ring[IM][(u + P - 1) % P][cpi * E], fm, true);
                 }
                 fa += PS;
                 fb += PS;
                 fc += PS;
+                fm += PS;
             }
             cp_async_commit();
             const bool act = st >= st_lo && st < st_hi;
@@ -965,10 +973,10 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
                 // _applyPreconditioner forward solve (pressuresolver.cpp:311-351); neighbours hand
                 // over (negscale*precon)*q; precon is 0 off the fluid set, so those cells give 0
                 val = Op::mul(Op::sub(Op::sub(Op::sub(ra, prev), nj_), nk_), pc);
-                xch = Op::mul(Op::mul(A.negscale, pc), val);
+                xch = Op::mul(PM ? ring[IM][u][tid] : Op::mul(A.negscale, pc), val);
             } else {
                 // backward solve (pressuresolver.cpp:354-385)
-                const T m = Op::mul(A.negscale, pc);
+                const T m = PM ? ring[IM][u][tid] : Op::mul(A.negscale, pc);
                 val = Op::mul(Op::sub(Op::sub(Op::sub(ra, Op::mul(m, prev)), Op::mul(m, nj_)), Op::mul(m, nk_)), pc);
                 xch = val;
             }
@@ -976,7 +984,7 @@ __global__ void __launch_bounds__(SPLANE + RX_THREADS, 1) k_tri(SweepArgs<T> A) 
             val = act ? val : T(0);
             xch = act ? xch : T(0);
             if (MODE == SW_BWD && act) {
-                const T rv = ring[NARR - 1][u][tid];
+                const T rv = ring[2][u][tid];
                 if (sizeof(T) == 4) dot32.add((float)val * (float)rv);
                 else dot64 += (double)val * (double)rv;
             }
@@ -2372,6 +2380,7 @@ static int launch_sweep(Ctx *ctx, PressureWs &ws, const T *in, T *out, const T *
     A.out = out;
     A.precon = precon;
     A.rdot = rdot;
+    A.mpc = sizeof(T) == 8 ? (const T *)ws.mpc.p : nullptr;
     A.out32 = out32;
     A.negscale = (T)(-scale);
     A.scale = scale;
@@ -2491,6 +2500,14 @@ static int read_ctrl(Ctx *ctx, PressureWs &ws, PsCtrl *h) {
 // inner PCG in FP32 with FP64 reliable updates of the residual.  Fills the
 // reference-numbered iteration count, the final max-norm residual, the number
 // of FP64 updates and of forward (= backward) MIC(0) solves.
+// mpc = negscale * precon over every slot, with the solves' own FP64 multiply
+__global__ void __launch_bounds__(RED_THREADS) k_neg_precon(long long n, double negscale,
+                                                            const double *__restrict__ precon,
+                                                            double *__restrict__ mpc) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        mpc[q] = Ar<double>::mul(negscale, precon[q]);
+}
+
 // The list of strips (of Strip<T>::W slots) that hold fluid, for this solve's vector kernels.
 template <class T>
 static int build_strip_list(Ctx *ctx, PressureWs &ws, const Skew &K) {
@@ -2522,6 +2539,13 @@ static int run_cg(Ctx *ctx, PressureWs &ws, const Skew &K, double scale, bool mi
     else rc = launch_sweep<double, SW_PRECON>(ctx, ws, nullptr, ws.precon.as<double>(), nullptr, nullptr, nullptr,
                                               scale, 0);
     if (rc) return rc;
+    if (!mixed) {
+        // negscale * precon for the FP64 triangular solves
+        if (ws.mpc.ensure((size_t)K.size * sizeof(double))) return GFS_ERR_NOMEM;
+        k_neg_precon<<<nb, RED_THREADS, 0, st>>>(K.size, -scale, ws.precon.as<double>(), ws.mpc.as<double>());
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+    }
     if (!mixed) {
         double *p = ws.psk.as<double>(), *r = ws.r.as<double>(), *z = ws.z.as<double>(),
                *s = ws.s.as<double>(), *As = ws.As.as<double>(), *q = ws.q.as<double>(),
