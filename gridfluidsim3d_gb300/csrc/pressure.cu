@@ -1781,6 +1781,7 @@ struct VecArgs {
     int mixed;
     const unsigned *slist;   // the strips (of Strip<T>::W slots) that hold fluid, in order
     const unsigned *snum;    // their number
+    T dcoef[8];              // (T)n * scale for n non-solid neighbours, formed once on the host
 };
 
 // x at the six neighbours of slot q in the skewed layout, in the reference's
@@ -2023,7 +2024,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_matvec(VecArgs<T> A, const T *_
         for (int e = 0; e < W; e++) {
             const unsigned fl = f.at(e);
             T v = Op::mul(val[e], A.negscale);
-            v = Op::add(v, Op::mul(Op::mul((T)(fl >> 1), A.scale), xc[e]));
+            v = Op::add(v, Op::mul(A.dcoef[(fl >> 1) & 7u], xc[e]));
             val[e] = v;
             if (fl & GFS_PF_FLUID) {
                 if (sizeof(T) == 4) dot32.add((float)v * (float)xc[e]);
@@ -2094,7 +2095,12 @@ __global__ void __launch_bounds__(RED_THREADS) k_update_s(VecArgs<T> A, const T 
         load_strip<T>(zv, z + q0);
         load_strip<T>(sv, s + q0);
 #pragma unroll
-        for (int e = 0; e < W; e++) sv[e] = Op::add(Op::mul(zv[e], (T)1.0), Op::mul(sv[e], beta));
+        for (int e = 0; e < W; e++) {
+            // FP64: z * 1 is z exactly, so the multiply is left out (GB300's FP64 rate);
+            // FP32 keeps the expression as compiled so far
+            if constexpr (sizeof(T) == 8) sv[e] = Op::add(zv[e], Op::mul(sv[e], beta));
+            else sv[e] = Op::add(Op::mul(zv[e], (T)1.0), Op::mul(sv[e], beta));
+        }
         store_strip_fluid<T>(s + q0, sv, f);
     }
 }
@@ -2210,7 +2216,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_residual64(VecArgs<double> A, c
             for (int e = 0; e < W; e++) {
                 const unsigned fl = f.at(e);
                 double v = Op::mul(val[e], A.negscale);
-                v = Op::add(v, Op::mul(Op::mul((double)(fl >> 1), A.scale), xc[e]));
+                v = Op::add(v, Op::mul(A.dcoef[(fl >> 1) & 7u], xc[e]));
                 val[e] = bv[e] - v;
                 if (fl & GFS_PF_FLUID) mx = fmax(mx, fabs(val[e]));
             }
@@ -2450,6 +2456,9 @@ static VecArgs<T> vec_args(PressureWs &ws, double scale, int mixed) {
     A.mixed = mixed;
     A.slist = ws.slist.as<unsigned>();
     A.snum = ws.snum.as<unsigned>();
+    // the diagonal coefficient of a cell with n non-solid neighbours, (T)n * scale, as the
+    // device forms it (one IEEE multiply in T)
+    for (int n = 0; n < 8; n++) A.dcoef[n] = (T)n * A.scale;
     return A;
 }
 
