@@ -7,9 +7,10 @@
 //               fluidsimulation.cpp:1933-1958) and an atomic slot in its cell;
 //   scan        exclusive scan of the per-cell counts -> cell offsets;
 //   k_scatter   particles to offset[cell] + slot;
-//   k_cell_sort insertion sort of each cell's run by particle id, which makes
-//               the order independent of the atomic slot order (the splat sums
-//               in this order, so every run is bitwise reproducible);
+//   k_rank_sort each particle of a cell's run to its rank by particle id in the
+//               run, which makes the order independent of the atomic slot
+//               order (the splat sums in this order, so every run is bitwise
+//               reproducible);
 //   cap         cells holding more than max_particles_per_cell keep their
 //               smallest ids (FluidSimulation::_removeMarkerParticles,
 //               fluidsimulation.cpp:3221-3243, keeps a random subset after a
@@ -75,31 +76,43 @@ __global__ void k_scatter(const float4 *__restrict__ pos, const float4 *__restri
     vel_out[d] = vel[p];
 }
 
-// One thread per cell: insertion sort of the cell's run by id, in place.
-__global__ void k_cell_sort(float4 *__restrict__ pos, float4 *__restrict__ vel,
-                            const uint32_t *__restrict__ offset, long long ncells, int cap,
-                            uint32_t *__restrict__ num) {
-    long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (c >= ncells) return;
-    uint32_t b = offset[c], e = offset[c + 1];
-    if (c == ncells - 1) num[0] = e;    // particle count after removal
-    uint32_t m = e - b;
-    if ((int)m > cap) atomicOr(&num[1], 1u);
-    if (m <= 1) return;
-    for (uint32_t a = b + 1; a < e; a++) {
-        float4 cp = pos[a];
-        uint32_t cid = pid(cp);
-        if (pid(pos[a - 1]) <= cid) continue;
-        float4 cv = vel[a];
-        uint32_t t = a;
-        while (t > b && pid(pos[t - 1]) > cid) {
-            pos[t] = pos[t - 1];
-            vel[t] = vel[t - 1];
-            t--;
-        }
-        pos[t] = cp;
-        vel[t] = cv;
+// One thread per particle of the scattered set: its place in its cell's run is its rank by
+// id there (ties, which distinct ids never give, by scattered position).  The (cell, id)
+// order is that of an insertion sort of each run by id, reached without a serial pass
+// per cell.  The cell is recomputed with k_keys' formula; num[0] gets the count after
+// removal and num[1] the flag of a cell holding more than cap particles.
+__global__ void k_rank_sort(const float4 *__restrict__ pos_in, const float4 *__restrict__ vel_in,
+                            const uint32_t *__restrict__ offset, long long ncells, long long nbound, GridDim c,
+                            double invdx_d, float invdx_f, int pow2, int cap, float4 *__restrict__ pos_out,
+                            float4 *__restrict__ vel_out, uint32_t *__restrict__ num) {
+    const long long n = (long long)offset[ncells];
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q == 0) num[0] = (uint32_t)n;
+    if (q >= n || q >= nbound) return;
+    const float4 x = pos_in[q];
+    int i, j, k;
+    if (pow2) {
+        i = (int)floorf(x.x * invdx_f);
+        j = (int)floorf(x.y * invdx_f);
+        k = (int)floorf(x.z * invdx_f);
+    } else {
+        i = (int)floor((double)x.x * invdx_d);
+        j = (int)floor((double)x.y * invdx_d);
+        k = (int)floor((double)x.z * invdx_d);
     }
+    if (!c.in(i, j, k)) return;   // never for a scattered set
+    const uint32_t kk = (uint32_t)i + (uint32_t)c.nx * ((uint32_t)j + (uint32_t)c.ny * (uint32_t)k);
+    const uint32_t b = offset[kk], e = offset[kk + 1];
+    if ((uint32_t)q < b || (uint32_t)q >= e) return;   // never for a scattered set
+    const uint32_t id = pid(x);
+    uint32_t r = 0;
+    for (uint32_t a = b; a < e; a++) {
+        const uint32_t o = pid(pos_in[a]);
+        r += (o < id || (o == id && a < (uint32_t)q)) ? 1u : 0u;
+    }
+    if (r == (uint32_t)cap) atomicOr(&num[1], 1u);   // the cell holds more than cap
+    pos_out[b + r] = x;
+    vel_out[b + r] = vel_in[q];
 }
 
 __global__ void k_cap_counts(const uint32_t *__restrict__ offset, long long ncells, int cap,
@@ -249,7 +262,7 @@ int exclusive_scan_u32(Ctx *ctx, uint32_t *in, uint32_t *out, long long n, uint3
 
 // --------------------------------------------------------------- driver
 
-// The cap check of k_cell_sort for a set that was already in order: num[0] = the
+// The cap check of k_rank_sort for a set that was already in order: num[0] = the
 // particle count after removal, num[1] set if a cell holds more than `cap`.
 __global__ void k_cap_flag(const uint32_t *__restrict__ offset, long long ncells, int cap,
                            uint32_t *__restrict__ num) {
@@ -338,7 +351,7 @@ int sort_particles(Sim *s, bool /*remove_solid*/) {
     // A set that is already in (cell, id) order with no particle to remove -- an
     // upload of the particles a step handed back, or a load of a saved state --
     // keeps its place: the offsets are all the sort has to produce.  The cap is
-    // then checked the way k_cell_sort checks it.
+    // then checked the way k_rank_sort checks it.
     bool in_order = false;
     if (s->sorted_hint && nb > 0) {
         k_check_sorted<<<grid_blocks(nb, T), T, 0, st>>>(s->pos.as<float4>(), s->key.as<uint32_t>(), num, nb,
@@ -366,11 +379,16 @@ int sort_particles(Sim *s, bool /*remove_solid*/) {
         ctx->launches++;
         GFS_LAUNCH_CHECK();
     }
-    std::swap(s->pos.p, s->pos_alt.p);
-    std::swap(s->vel.p, s->vel_alt.p);
     int cap = s->params.max_particles_per_cell > 0 ? s->params.max_particles_per_cell : 0x7fffffff;
-    k_cell_sort<<<grid_blocks(ncells, T), T, 0, st>>>(s->pos.as<float4>(), s->vel.as<float4>(),
-                                                      offset, ncells, cap, num);
+    if (nb > 0) {
+        // the scattered set (pos_alt) into (cell, id) order, back into pos
+        k_rank_sort<<<grid_blocks(nb, T), T, 0, st>>>(s->pos_alt.as<float4>(), s->vel_alt.as<float4>(), offset,
+                                                      ncells, nb, c, 1.0 / s->g.dx, s->inv_dx_f,
+                                                      s->dx_pow2 ? 1 : 0, cap, s->pos.as<float4>(),
+                                                      s->vel.as<float4>(), num);
+    } else {
+        k_cap_flag<<<grid_blocks(ncells, T), T, 0, st>>>(offset, ncells, cap, num);
+    }
     ctx->launches++;
     GFS_LAUNCH_CHECK();
     return finish_sort(s, ncells, false);
