@@ -79,15 +79,17 @@ __global__ void k_scatter(const float4 *__restrict__ pos, const float4 *__restri
 // One thread per particle of the scattered set: its place in its cell's run is its rank by
 // id there (ties, which distinct ids never give, by scattered position).  The (cell, id)
 // order is that of an insertion sort of each run by id, reached without a serial pass
-// per cell.  The cell is recomputed with k_keys' formula; num[0] gets the count after
-// removal and num[1] the flag of a cell holding more than cap particles.
+// per cell.  The cell is recomputed with k_keys' formula.  A cell keeps its `cap` smallest
+// ids, written from dst_off (the scan of min(count, cap); the run offsets themselves when no
+// cap applies), and num[0] gets the count after removal and capping.
 __global__ void k_rank_sort(const float4 *__restrict__ pos_in, const float4 *__restrict__ vel_in,
-                            const uint32_t *__restrict__ offset, long long ncells, long long nbound, GridDim c,
-                            double invdx_d, float invdx_f, int pow2, int cap, float4 *__restrict__ pos_out,
-                            float4 *__restrict__ vel_out, uint32_t *__restrict__ num) {
+                            const uint32_t *__restrict__ offset, const uint32_t *__restrict__ dst_off,
+                            long long ncells, long long nbound, GridDim c, double invdx_d, float invdx_f, int pow2,
+                            int cap, float4 *__restrict__ pos_out, float4 *__restrict__ vel_out,
+                            uint32_t *__restrict__ num) {
     const long long n = (long long)offset[ncells];
     const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (q == 0) num[0] = (uint32_t)n;
+    if (q == 0) num[0] = dst_off[ncells];
     if (q >= n || q >= nbound) return;
     const float4 x = pos_in[q];
     int i, j, k;
@@ -110,9 +112,10 @@ __global__ void k_rank_sort(const float4 *__restrict__ pos_in, const float4 *__r
         const uint32_t o = pid(pos_in[a]);
         r += (o < id || (o == id && a < (uint32_t)q)) ? 1u : 0u;
     }
-    if (r == (uint32_t)cap) atomicOr(&num[1], 1u);   // the cell holds more than cap
-    pos_out[b + r] = x;
-    vel_out[b + r] = vel_in[q];
+    if (r >= (uint32_t)cap) return;   // the cell's smallest ids stay (dst_off: the capped run starts)
+    const uint32_t d = dst_off[kk] + r;
+    pos_out[d] = x;
+    vel_out[d] = vel_in[q];
 }
 
 __global__ void k_cap_counts(const uint32_t *__restrict__ offset, long long ncells, int cap,
@@ -381,16 +384,29 @@ int sort_particles(Sim *s, bool /*remove_solid*/) {
     }
     int cap = s->params.max_particles_per_cell > 0 ? s->params.max_particles_per_cell : 0x7fffffff;
     if (nb > 0) {
+        // with a cap, the capped run starts: the scan of min(count, cap), into `count`
+        // (FluidSimulation::_removeMarkerParticles, fluidsimulation.cpp:3221-3243)
+        const bool capping = s->params.max_particles_per_cell > 0;
+        if (capping) {
+            k_cap_counts<<<grid_blocks(ncells + 1, T), T, 0, st>>>(offset, ncells, cap, count);
+            ctx->launches++;
+            GFS_LAUNCH_CHECK();
+            rc = exclusive_scan_u32(ctx, count, count, ncells + 1, s->scan_tmp.as<uint32_t>(), st);
+            if (rc) return rc;
+        }
         // the scattered set (pos_alt) into (cell, id) order, back into pos
         k_rank_sort<<<grid_blocks(nb, T), T, 0, st>>>(s->pos_alt.as<float4>(), s->vel_alt.as<float4>(), offset,
-                                                      ncells, nb, c, 1.0 / s->g.dx, s->inv_dx_f,
-                                                      s->dx_pow2 ? 1 : 0, cap, s->pos.as<float4>(),
+                                                      capping ? count : offset, ncells, nb, c, 1.0 / s->g.dx,
+                                                      s->inv_dx_f, s->dx_pow2 ? 1 : 0, cap, s->pos.as<float4>(),
                                                       s->vel.as<float4>(), num);
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
+        if (capping) std::swap(s->count.p, s->offset.p);   // the capped starts become the live offsets
     } else {
         k_cap_flag<<<grid_blocks(ncells, T), T, 0, st>>>(offset, ncells, cap, num);
+        ctx->launches++;
+        GFS_LAUNCH_CHECK();
     }
-    ctx->launches++;
-    GFS_LAUNCH_CHECK();
     return finish_sort(s, ncells, false);
 }
 
