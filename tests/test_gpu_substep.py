@@ -239,3 +239,25 @@ def test_context_closed_before_its_simulation():
         ctx.close()
     for a, b in zip(out[0], out[1]):
         assert np.array_equal(a, b)
+
+
+def test_duplicate_ids_lose_no_particle(gpu_ctx):
+    """Particles are ordered by (cell, id); ids a caller repeats tie-break by position in
+    the scattered set, so every particle keeps a slot of its own: the same count after a
+    substep as with distinct ids, finite state, and every returned id one of the input ids."""
+    sc = scenes.random_box(dims=(16, 12, 14), seed=2)
+    counts = []
+    for dup in (False, True):
+        ids = sc.ids.copy()
+        if dup:
+            ids[1::2] = ids[0::2][:len(ids[1::2])]   # neighbours in the input share an id
+        sim = FluidSimulation(*sc.dims, sc.dx, max_particles=sc.num_particles, ctx=gpu_ctx)
+        sim.set_material_grid(sc.mat)
+        sim.set_marker_particles(sc.pos, sc.vel, ids)
+        sim.update(sc.dt)
+        pos, vel, out = sim.get_marker_particles()
+        assert np.isfinite(pos).all() and np.isfinite(vel).all()
+        assert np.isin(out, ids).all()
+        counts.append(len(out))
+        sim.close()
+    assert counts[0] == counts[1] and counts[0] > 0
